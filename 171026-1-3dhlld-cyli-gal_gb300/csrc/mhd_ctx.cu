@@ -1,0 +1,656 @@
+/*
+ * mhd_ctx.cu -- the C-ABI of libmhdgpu.so (include/mhd_gpu.h): context
+ * set-up, state transfer, and the step orchestration on one CUDA stream.
+ *
+ * Reference call chain replaced (main.c:316-393):
+ *   Setdt()          -> mhd_setdt()          (setdt.h:24-94)
+ *   SpiralGravity()  -> mhd_spiral_gravity() (spiralgravity.h:20-124)
+ *   TVDRK()          -> mhd_tvdrk()          (tvdrungekutta.h:16-78)
+ *
+ * Device data layout: the reference's own, [m][i][j][k] with k fastest and one
+ * ghost cell per side, so host<->device copies are plain memcpy.  The
+ * j-independent grid tables (geometric factors, minimum cell length,
+ * axisymmetric gravity) are stored once per (i,k).  Compiled with
+ * --fmad=false (the gravity probe and the FP64 scalars must round as the
+ * reference does).
+ */
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "mhd_launch.h"
+
+using namespace mhd;
+
+struct mhd_ctx {
+    int device;
+    cudaStream_t st;
+    mhd_params p;
+    int ix, jy, kz, ixmax, jymax, kzmax, irin;
+    long long nc;
+    int fp32;
+    size_t esz;
+    Geom G;
+    double *dtab;
+    float *ftab;
+    void *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
+    int vcur;
+    StepScalars *d_sc, *h_sc;
+    double *d_trig, *h_trig;
+    MaxLoc *d_part, *h_part;
+    int npart;
+    int *d_cnt, *h_cnt;
+    double *d_stage;
+    long long stage_n;
+    std::vector<double> hx, hy, hspL;
+    double omdiff;
+    int uploaded;
+    cudaError_t last_cuda;
+    /* mhd_run graph */
+    cudaGraphExec_t gexec;
+    int graph_ready;
+    int *d_cnt_run;
+};
+
+#define CK(call)                                   \
+    do {                                           \
+        cudaError_t e_ = (call);                   \
+        if (e_ != cudaSuccess) {                   \
+            if (ctx) ctx->last_cuda = e_;          \
+            return MHD_ERR_CUDA;                   \
+        }                                          \
+    } while (0)
+
+static void *vcur_ptr(mhd_ctx *ctx) { return ctx->vcur == 0 ? ctx->Va : ctx->Vb; }
+static void *vnext_ptr(mhd_ctx *ctx) { return ctx->vcur == 0 ? ctx->Vb : ctx->Va; }
+
+/* ------------------------------------------------------------------------ */
+/* small kernels that live here                                              */
+/* ------------------------------------------------------------------------ */
+
+/* cos/sin of the arm phase per (i,j) (spiralgravity.h:63-65) on the device,
+ * for the precision form; the plain form fills the same table on the host
+ * with the C library's sincos, the function the reference calls. */
+__global__ void trig_kernel(int ixmax, int jymax, const double *__restrict__ y, const double *__restrict__ spL,
+                            double armnum, double omdiff, const StepScalars *__restrict__ sc, double *trig)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)ixmax * jymax) return;
+    int i = (int)(t / jymax), j = (int)(t % jymax);
+    double phase = armnum * (y[j] - omdiff * sc->t + spL[i]);
+    double s, c;
+    sincos(phase, &s, &c);
+    trig[t] = c;
+    trig[(long long)ixmax * jymax + t] = s;
+}
+
+__global__ void gravity_probe_kernel(Geom G, const StepScalars *__restrict__ sc, const double *__restrict__ trig,
+                                     double *out)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G.nc) return;
+    int k = (int)(t % G.kzmax);
+    long long r = t / G.kzmax;
+    int j = (int)(r % G.jymax), i = (int)(r / G.jymax);
+    double gx, gy, gz;
+    gravity_field(G, *sc, trig, i, j, k, gx, gy, gz);
+    out[t] = gx;
+    out[G.nc + t] = gy;
+    out[2 * G.nc + t] = gz;
+}
+
+/* ------------------------------------------------------------------------ */
+/* host helpers                                                              */
+/* ------------------------------------------------------------------------ */
+static int check_grid(const mhd_grid *g)
+{
+    if (!g || g->ix < 12 || g->kz < 12 || g->jy < 4 || (g->jy & 1)) return MHD_ERR_ARG;
+    if (!g->x || !g->xm || !g->oneox || !g->oneodx || !g->y || !g->z || !g->oneodz || !g->dzm) return MHD_ERR_ARG;
+    if (!g->g1 || !g->g2 || !g->g3 || !g->g4 || !g->g5 || !g->g6 || !g->minlength) return MHD_ERR_ARG;
+    if (!g->x_absorb_factor || !g->z_absorb_factor || !g->c_absorb_factor) return MHD_ERR_ARG;
+    if (g->irin < 0 || g->irin > g->ix) return MHD_ERR_ARG;
+    return MHD_OK;
+}
+
+/* gather a j-independent table into [ni][nk]; returns MHD_ERR_ARG if a
+ * reference-layout table actually varies with j over [j0, j1) */
+static int gather_ik(const double *src, int compact, int ni, int nj, int nk, int j0, int j1, double *dst, int dst_nk)
+{
+    for (int i = 0; i < ni; i++)
+        for (int k = 0; k < nk; k++) {
+            double v;
+            if (compact) v = src[(size_t)i * nk + k];
+            else {
+                v = src[((size_t)i * nj + j0) * nk + k];
+                for (int j = j0 + 1; j < j1; j++)
+                    if (memcmp(&src[((size_t)i * nj + j) * nk + k], &v, sizeof v) != 0) return MHD_ERR_ARG;
+            }
+            dst[(size_t)i * dst_nk + k] = v;
+        }
+    return MHD_OK;
+}
+
+static void free_all(mhd_ctx *ctx)
+{
+    void *dev[] = {ctx->dtab, ctx->ftab, ctx->U, ctx->U1, ctx->Va, ctx->Vb, ctx->Uinit, ctx->Vinit,
+                   ctx->rhofloor, ctx->F, ctx->Gf, ctx->H, ctx->Uraw, ctx->d_sc, ctx->d_trig,
+                   ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run};
+    for (size_t q = 0; q < sizeof dev / sizeof dev[0]; q++)
+        if (dev[q]) cudaFree(dev[q]);
+    if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
+    if (ctx->h_trig) cudaFreeHost(ctx->h_trig);
+    if (ctx->h_part) cudaFreeHost(ctx->h_part);
+    if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+}
+
+/* ------------------------------------------------------------------------ */
+/* create / destroy                                                          */
+/* ------------------------------------------------------------------------ */
+extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
+{
+    mhd_ctx *ctx = NULL;
+    if (!out || !p) return MHD_ERR_ARG;
+    *out = NULL;
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (p->limiter < 0 || p->limiter > 1 || p->solver < 0 || p->solver > 1 ||
+        (p->scheme != MHD_SCHEME_RK2 && p->scheme != MHD_SCHEME_RK3) || p->precision < 0 || p->precision > 1)
+        return MHD_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return MHD_ERR_NODEV;
+
+    ctx = new (std::nothrow) mhd_ctx();
+    if (!ctx) return MHD_ERR_NOMEM;
+    memset((void *)&ctx->G, 0, sizeof ctx->G);
+    cudaGetDevice(&ctx->device);
+    ctx->p = *p;
+    ctx->ix = g->ix; ctx->jy = g->jy; ctx->kz = g->kz;
+    ctx->ixmax = g->ix + 2; ctx->jymax = g->jy + 2; ctx->kzmax = g->kz + 2;
+    ctx->irin = g->irin;
+    ctx->nc = (long long)ctx->ixmax * ctx->jymax * ctx->kzmax;
+    ctx->fp32 = p->precision == MHD_PREC_FP32;
+    ctx->esz = ctx->fp32 ? sizeof(float) : sizeof(double);
+    const int ixmax = ctx->ixmax, jymax = ctx->jymax, kzmax = ctx->kzmax;
+    const long long nc = ctx->nc;
+
+    /* ---- host tables ---- */
+    const size_t nik = (size_t)ixmax * kzmax;
+    std::vector<double> gtab(6 * nik, 0.0), minl(nik), grax(3 * nik, 0.0);
+    const double *gsrc[6] = {g->g1, g->g2, g->g3, g->g4, g->g5, g->g6};
+    for (int n = 0; n < 6; n++) {
+        /* face-shaped [ixmax-1][jymax-1][kzmax-1]; rows j=0 are never read */
+        rc = gather_ik(gsrc[n], g->compact, ixmax - 1, jymax - 1, kzmax - 1, 1, jymax - 1, &gtab[n * nik], kzmax);
+        if (rc) { delete ctx; return rc; }
+    }
+    rc = gather_ik(g->minlength, g->compact, ixmax, jymax, kzmax, 0, jymax, minl.data(), kzmax);
+    if (rc) { delete ctx; return rc; }
+    const double *gr[3] = {g->Grxaxi, g->Gryaxi, g->Grzaxi};
+    for (int n = 0; n < 3; n++)
+        if (gr[n]) {
+            rc = gather_ik(gr[n], g->compact, ixmax, jymax, kzmax, 0, jymax, &grax[n * nik], kzmax);
+            if (rc) { delete ctx; return rc; }
+        }
+
+    /* spiral tables (spiralgravity.h:37-77), C-library math as the reference */
+    const double a1 = 0.65, b1 = 0.026;
+    double oneoscalephase = 1.0 / p->scalephase, oneoscaler = 1.0 / p->scaler;
+    double cotpitch = 1.0 / tan(p->pitch);
+    std::vector<double> spA(nik), spS(kzmax), spQ(kzmax), spR(kzmax), spC1(ixmax), spC2(ixmax), spD(ixmax),
+        spL(ixmax);
+    for (int i = 0; i < ixmax; i++) {
+        double xi = g->x[i];
+        double xoscalephase = xi * oneoscalephase;
+        double xoscaler = xi * oneoscaler;
+        double xoscaler2 = xoscaler * oneoscaler;
+        double x2oscaler2 = xoscaler * xoscaler;
+        double oneoonex2oscaler2 = 1.0 / (1.0 + x2oscaler2);
+        double oneoonex2oscaler215 = 1.0 * pow(oneoonex2oscaler2, 1.5);
+        spC1[i] = xoscaler2 * oneoonex2oscaler215;
+        spC2[i] = x2oscaler2 * oneoonex2oscaler215;
+        spD[i] = ((2.0 - x2oscaler2) * oneoonex2oscaler2);
+        spL[i] = cotpitch * log(xoscalephase);
+        double x2 = xi * xi;
+        for (int k = 0; k < kzmax; k++) {
+            double z2 = g->z[k] * g->z[k];
+            double a1zk2b12 = ((a1 + sqrt(z2 + b1 * b1)) * (a1 + sqrt(z2 + b1 * b1)));
+            spA[(size_t)i * kzmax + k] = 1.0 / sqrt(x2 + a1zk2b12);
+        }
+    }
+    for (int k = 0; k < kzmax; k++) {
+        double z2 = g->z[k] * g->z[k];
+        spS[k] = (p->scalez / sqrt(z2 + p->scalez * p->scalez));
+        spQ[k] = (1.0 + a1 / sqrt(z2 + b1 * b1));
+        spR[k] = 1.0 / (z2 + p->scalez * p->scalez);
+    }
+    ctx->hx.assign(g->x, g->x + ixmax);
+    ctx->hy.assign(g->y, g->y + jymax);
+    ctx->hspL = spL;
+    ctx->omdiff = p->omegapattern - p->omegasp;
+
+    /* ---- pack double tables ---- */
+    std::vector<double> T;
+    auto put = [&](const double *src, size_t n) { size_t off = T.size(); T.insert(T.end(), src, src + n); return off; };
+    std::vector<double> oneodz(g->oneodz, g->oneodz + kzmax);
+    size_t o_x = put(g->x, ixmax), o_xm = put(g->xm, ixmax), o_ox = put(g->oneox, ixmax);
+    size_t o_odx = put(g->oneodx, ixmax), o_odz = put(oneodz.data(), kzmax);
+    size_t o_g = put(gtab.data(), 6 * nik);
+    size_t o_xabs = put(g->x_absorb_factor, 11), o_zabs = put(g->z_absorb_factor, 11);
+    size_t o_cabs = put(g->c_absorb_factor, (size_t)(g->irin + 1) * kzmax);
+    size_t o_minl = put(minl.data(), nik), o_grax = put(grax.data(), 3 * nik);
+    size_t o_spA = put(spA.data(), nik), o_spS = put(spS.data(), kzmax), o_spQ = put(spQ.data(), kzmax);
+    size_t o_spR = put(spR.data(), kzmax), o_C1 = put(spC1.data(), ixmax), o_C2 = put(spC2.data(), ixmax);
+    size_t o_D = put(spD.data(), ixmax), o_L = put(spL.data(), ixmax), o_y = put(g->y, jymax);
+    size_t o_z = put(g->z, kzmax);
+    size_t nfl = (size_t)(o_cabs + (size_t)(g->irin + 1) * kzmax);   /* float copies: up to cabs */
+    std::vector<float> TF(T.begin(), T.begin() + nfl);
+
+#define CKC(call)                                  \
+    do {                                           \
+        cudaError_t e_ = (call);                   \
+        if (e_ != cudaSuccess) {                   \
+            free_all(ctx); delete ctx;             \
+            return e_ == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; \
+        }                                          \
+    } while (0)
+
+    CKC(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+    CKC(cudaMalloc((void **)&ctx->dtab, T.size() * sizeof(double)));
+    CKC(cudaMalloc((void **)&ctx->ftab, TF.size() * sizeof(float)));
+    CKC(cudaMemcpy(ctx->dtab, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CKC(cudaMemcpy(ctx->ftab, TF.data(), TF.size() * sizeof(float), cudaMemcpyHostToDevice));
+
+    Geom &G = ctx->G;
+    G.ixmax = ixmax; G.jymax = jymax; G.kzmax = kzmax; G.jy = g->jy; G.irin = g->irin; G.nc = nc;
+    double *D = ctx->dtab;
+    float *Fd = ctx->ftab;
+    G.d.x = D + o_x; G.d.xm = D + o_xm; G.d.oneox = D + o_ox; G.d.oneodx = D + o_odx; G.d.oneodz = D + o_odz;
+    G.d.g = D + o_g; G.d.xabs = D + o_xabs; G.d.zabs = D + o_zabs; G.d.cabs = D + o_cabs; G.d.oneody = g->oneody;
+    G.f.x = Fd + o_x; G.f.xm = Fd + o_xm; G.f.oneox = Fd + o_ox; G.f.oneodx = Fd + o_odx; G.f.oneodz = Fd + o_odz;
+    G.f.g = Fd + o_g; G.f.xabs = Fd + o_xabs; G.f.zabs = Fd + o_zabs; G.f.cabs = Fd + o_cabs;
+    G.f.oneody = (float)g->oneody;
+    G.minlength = D + o_minl; G.minminlength = g->minminlength; G.graxi = D + o_grax;
+    G.spA = D + o_spA; G.spS = D + o_spS; G.spQ = D + o_spQ; G.spR = D + o_spR;
+    G.spC1 = D + o_C1; G.spC2 = D + o_C2; G.spD = D + o_D; G.spL = D + o_L; G.y = D + o_y; G.z = D + o_z;
+    G.omegasp = p->omegasp; G.prcr = p->prcr; G.betacr = p->betacr; G.rhocr = p->rhocr;
+    G.armnum = (double)p->armnum; G.cotpitch = cotpitch;
+    G.cooling = p->cooling; G.gravity = p->gravity; G.limiter = p->limiter; G.solver = p->solver;
+    G.scheme = p->scheme;
+    G.repair_irmax = ctx->fp32 ? 4 : 0;
+
+    /* ---- state ---- */
+    size_t s9 = 9 * (size_t)nc * ctx->esz;
+    void **bufs9[] = {&ctx->U, &ctx->U1, &ctx->Va, &ctx->Vb, &ctx->Uinit, &ctx->Vinit, &ctx->F, &ctx->Gf, &ctx->H,
+                      &ctx->Uraw};
+    for (size_t q = 0; q < sizeof bufs9 / sizeof bufs9[0]; q++) {
+        CKC(cudaMalloc(bufs9[q], s9));
+        CKC(cudaMemsetAsync(*bufs9[q], 0, s9, ctx->st));
+    }
+    CKC(cudaMalloc(&ctx->rhofloor, (size_t)nc * ctx->esz));
+    CKC(cudaMalloc((void **)&ctx->d_sc, sizeof(StepScalars)));
+    CKC(cudaMallocHost((void **)&ctx->h_sc, sizeof(StepScalars)));
+    memset(ctx->h_sc, 0, sizeof(StepScalars));
+    CKC(cudaMemcpy(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice));
+    size_t ntrig = 2 * (size_t)ixmax * jymax;
+    CKC(cudaMalloc((void **)&ctx->d_trig, ntrig * sizeof(double)));
+    CKC(cudaMemset(ctx->d_trig, 0, ntrig * sizeof(double)));
+    CKC(cudaMallocHost((void **)&ctx->h_trig, ntrig * sizeof(double)));
+    long long ndt = (long long)(ixmax - 12) * (jymax - 2) * (kzmax - 2);
+    ctx->npart = (int)((ndt + 255) / 256);
+    if (ctx->npart > 2048) ctx->npart = 2048;
+    if (ctx->npart < 1) ctx->npart = 1;
+    CKC(cudaMalloc((void **)&ctx->d_part, ctx->npart * sizeof(MaxLoc)));
+    CKC(cudaMallocHost((void **)&ctx->h_part, ctx->npart * sizeof(MaxLoc)));
+    CKC(cudaMalloc((void **)&ctx->d_cnt, 3 * 3 * sizeof(int)));
+    CKC(cudaMallocHost((void **)&ctx->h_cnt, 3 * 3 * sizeof(int)));
+    ctx->stage_n = 1LL << 24;
+    if (ctx->fp32) CKC(cudaMalloc((void **)&ctx->d_stage, ctx->stage_n * sizeof(double)));
+    CKC(cudaStreamSynchronize(ctx->st));
+#undef CKC
+    *out = ctx;
+    return MHD_OK;
+}
+
+extern "C" void mhd_destroy(mhd_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->st);
+    free_all(ctx);
+    delete ctx;
+}
+
+extern "C" void *mhd_stream(mhd_ctx *ctx) { return ctx ? (void *)ctx->st : NULL; }
+
+/* ------------------------------------------------------------------------ */
+/* transfers                                                                 */
+/* ------------------------------------------------------------------------ */
+/* host FP64 -> device state of the context's type */
+static int put_state(mhd_ctx *ctx, void *dst, const double *src, long long n)
+{
+    if (!ctx->fp32) {
+        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+        return MHD_OK;
+    }
+    for (long long off = 0; off < n; off += ctx->stage_n) {
+        long long m = n - off < ctx->stage_n ? n - off : ctx->stage_n;
+        CK(cudaMemcpyAsync(ctx->d_stage, src + off, m * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+        CK(launch_cvt(ctx->d_stage, (float *)dst + off, m, ctx->st));
+    }
+    return MHD_OK;
+}
+
+static int get_state(mhd_ctx *ctx, double *dst, const void *src, long long n)
+{
+    if (!ctx->fp32) {
+        CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+        return MHD_OK;
+    }
+    for (long long off = 0; off < n; off += ctx->stage_n) {
+        long long m = n - off < ctx->stage_n ? n - off : ctx->stage_n;
+        CK(launch_cvt_back((const float *)src + off, ctx->d_stage, m, ctx->st));
+        CK(cudaMemcpyAsync(dst + off, ctx->d_stage, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    return MHD_OK;
+}
+
+extern "C" int mhd_upload(mhd_ctx *ctx, const double *U, const double *V, const double *Uinit, const double *Vinit,
+                          const double *rhofloor)
+{
+    if (!ctx || !U || !V) return MHD_ERR_ARG;
+    long long n9 = 9 * ctx->nc;
+    int rc;
+    if ((rc = put_state(ctx, ctx->U, U, n9))) return rc;
+    ctx->vcur = 0;
+    if ((rc = put_state(ctx, ctx->Va, V, n9))) return rc;
+    if ((rc = put_state(ctx, ctx->Uinit, Uinit ? Uinit : U, n9))) return rc;
+    if ((rc = put_state(ctx, ctx->Vinit, Vinit ? Vinit : V, n9))) return rc;
+    std::vector<double> rf;
+    if (!rhofloor) {   /* SaveInitial: rhofloor = U[0]*rhocr (saveinitial.h:40) */
+        rf.resize(ctx->nc);
+        for (long long q = 0; q < ctx->nc; q++) rf[q] = U[q] * ctx->p.rhocr;
+        rhofloor = rf.data();
+    }
+    if ((rc = put_state(ctx, ctx->rhofloor, rhofloor, ctx->nc))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->uploaded = 1;
+    return MHD_OK;
+}
+
+extern "C" int mhd_download(mhd_ctx *ctx, double *U, double *V)
+{
+    if (!ctx) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    int rc;
+    if (U && (rc = get_state(ctx, U, ctx->U, 9 * ctx->nc))) return rc;
+    if (V && (rc = get_state(ctx, V, vcur_ptr(ctx), 9 * ctx->nc))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return MHD_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Setdt                                                                     */
+/* ------------------------------------------------------------------------ */
+static MaxLoc better_host(MaxLoc a, MaxLoc b)
+{
+    if (b.q < 0) return a;
+    if (a.q < 0) return b;
+    if (b.v > a.v || (b.v == a.v && b.q < a.q)) return b;
+    return a;
+}
+
+extern "C" int mhd_setdt(mhd_ctx *ctx, double *dt, double *ch, int ijk[3])
+{
+    if (!ctx || !dt || !ch) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    if (ctx->fp32) CK(launch_setdt(ctx->G, (const float *)vcur_ptr(ctx), ctx->d_part, ctx->npart, ctx->st));
+    else CK(launch_setdt(ctx->G, (const double *)vcur_ptr(ctx), ctx->d_part, ctx->npart, ctx->st));
+    CK(cudaMemcpyAsync(ctx->h_part, ctx->d_part, ctx->npart * sizeof(MaxLoc), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    MaxLoc best = {0.0, -1};
+    for (int b = 0; b < ctx->npart; b++) best = better_host(best, ctx->h_part[b]);
+    double oneocfldt = best.q >= 0 ? best.v : 0.0;
+    /* setdt.h:84,89 */
+    *dt = ctx->p.cfl / oneocfldt;
+    *ch = ctx->G.minminlength * oneocfldt;
+    if (ijk) {
+        if (best.q < 0) { ijk[0] = ijk[1] = ijk[2] = -1; }
+        else {
+            ijk[2] = (int)(best.q % ctx->kzmax);
+            ijk[1] = (int)((best.q / ctx->kzmax) % ctx->jymax);
+            ijk[0] = (int)(best.q / ((long long)ctx->kzmax * ctx->jymax));
+        }
+    }
+    return MHD_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* SpiralGravity                                                             */
+/* ------------------------------------------------------------------------ */
+extern "C" int mhd_spiral_gravity(mhd_ctx *ctx, double t)
+{
+    if (!ctx) return MHD_ERR_ARG;
+    const mhd_params *p = &ctx->p;
+    /* spiralgravity.h:41-42 */
+    double switchfunc = (t - p->tausp) / fabs(t - p->tausp);
+    double epssp = 0.5 * p->epssp0 * (t / p->tausp * (1.0 - switchfunc) + (1.0 + switchfunc));
+    ctx->h_sc->epssp = epssp;
+    ctx->h_sc->t = t;
+    if (!p->gravity) return MHD_OK;
+    const int ixmax = ctx->ixmax, jymax = ctx->jymax;
+    if (!ctx->fp32) {
+        /* spiralgravity.h:63-65 with the C library's sincos */
+        CK(cudaStreamSynchronize(ctx->st));   /* h_trig may still feed a copy in flight */
+        double armnum = (double)p->armnum;
+        for (int i = 0; i < ixmax; i++)
+            for (int j = 0; j < jymax; j++) {
+                double phase = armnum * (ctx->hy[j] - ctx->omdiff * t + ctx->hspL[i]);
+                double s, c;
+                sincos(phase, &s, &c);
+                ctx->h_trig[(size_t)i * jymax + j] = c;
+                ctx->h_trig[(size_t)ixmax * jymax + (size_t)i * jymax + j] = s;
+            }
+        CK(cudaMemcpyAsync(ctx->d_trig, ctx->h_trig, 2 * (size_t)ixmax * jymax * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->st));
+    } else {
+        CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
+        long long n = (long long)ixmax * jymax;
+        trig_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->st>>>(ixmax, jymax, ctx->G.y, ctx->G.spL,
+                                                                       (double)p->armnum, ctx->omdiff, ctx->d_sc,
+                                                                       ctx->d_trig);
+        CK(cudaGetLastError());
+    }
+    return MHD_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* TVDRK                                                                     */
+/* ------------------------------------------------------------------------ */
+static Box flux_box(const mhd_ctx *ctx, int dir)
+{
+    Box b;
+    b.i0 = dir == 0 ? 0 : 1; b.i1 = ctx->ixmax - 1;
+    b.j0 = dir == 1 ? 0 : 1; b.j1 = ctx->jymax - 1;
+    b.k0 = dir == 2 ? 0 : 1; b.k1 = ctx->kzmax - 1;
+    return b;
+}
+
+template <typename T>
+static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
+{
+    const T *V = (const T *)vcur_ptr(ctx);
+    const T *Vinit = (const T *)ctx->Vinit;
+    T *F = (T *)ctx->F, *Gf = (T *)ctx->Gf, *H = (T *)ctx->H;
+    CK(launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
+    CK(launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
+    CK(launch_flux(2, ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), false, ctx->st));
+    StageArgs<T> a;
+    a.V = V; a.F = F; a.G = Gf; a.H = H;
+    a.Un = (T *)ctx->U; a.U1 = (T *)ctx->U1;
+    a.Uinit = (const T *)ctx->Uinit; a.rhofloor = (const T *)ctx->rhofloor;
+    a.Vout = (T *)vnext_ptr(ctx); a.Uraw = (T *)ctx->Uraw;
+    a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.kind = kind; a.last = last; a.counters = counters;
+    CK(launch_update(ctx->G, a, ctx->st));
+    ctx->vcur ^= 1;
+    return MHD_OK;
+}
+
+static int run_stages(mhd_ctx *ctx, int *d_cnt)
+{
+    static const int rk3[3][2] = {{0, 0}, {1, 0}, {2, 1}};
+    static const int rk2[2][2] = {{0, 0}, {3, 1}};
+    int ns = ctx->p.scheme == MHD_SCHEME_RK2 ? 2 : 3;
+    for (int s = 0; s < ns; s++) {
+        int kind = ns == 2 ? rk2[s][0] : rk3[s][0], last = ns == 2 ? rk2[s][1] : rk3[s][1];
+        int rc = ctx->fp32 ? run_stage<float>(ctx, kind, last, d_cnt + 3 * s)
+                           : run_stage<double>(ctx, kind, last, d_cnt + 3 * s);
+        if (rc) return rc;
+    }
+    return MHD_OK;
+}
+
+extern "C" int mhd_tvdrk(mhd_ctx *ctx, double dt, double ch, int counters[3])
+{
+    if (!ctx) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    StepScalars *h = ctx->h_sc;
+    h->dt = dt;
+    h->ch = ch;
+    /* tvdrungekutta.h:33-34 (RK3 factor 1/3, live RK2 factor 1/2) */
+    h->psicoef = ctx->p.scheme == MHD_SCHEME_RK2 ? exp(-dt * ch * MHD_ONEOCR * 0.5)
+                                                 : exp(-dt * ch * MHD_ONEOCR * MHD_ONEO3);
+    h->dtbad = 0;
+    CK(cudaMemcpyAsync(ctx->d_sc, h, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_cnt, 0, 9 * sizeof(int), ctx->st));
+    int rc = run_stages(ctx, ctx->d_cnt);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, 9 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    int last = ctx->p.scheme == MHD_SCHEME_RK2 ? 1 : 2;
+    if (counters) for (int c = 0; c < 3; c++) counters[c] = ctx->h_cnt[3 * last + c];
+    return MHD_OK;
+}
+
+extern "C" int mhd_step(mhd_ctx *ctx, double *t, double *dt, double *ch, int counters[3])
+{
+    if (!ctx || !t) return MHD_ERR_ARG;
+    double dtv, chv;
+    int rc = mhd_setdt(ctx, &dtv, &chv, NULL);
+    if (rc) return rc;
+    if (dt) *dt = dtv;
+    if (ch) *ch = chv;
+    if (isinf(dtv) || dtv < ctx->p.dtmin) return MHD_ERR_DT;   /* main.c:331 */
+    if (ctx->p.gravity && (rc = mhd_spiral_gravity(ctx, *t))) return rc;
+    if ((rc = mhd_tvdrk(ctx, dtv, chv, counters))) return rc;
+    *t = *t + dtv;
+    return MHD_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* probes                                                                    */
+/* ------------------------------------------------------------------------ */
+static Box full_face_box(const mhd_ctx *ctx)
+{
+    Box b = {0, ctx->ixmax - 1, 0, ctx->jymax - 1, 0, ctx->kzmax - 1};
+    return b;
+}
+
+extern "C" int mhd_dbg_limiter(mhd_ctx *ctx, int dir, double dt, double *Vl, double *Vr)
+{
+    if (!ctx || dir < 0 || dir > 2 || !Vl || !Vr) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    ctx->h_sc->dt = dt;
+    ctx->h_sc->psicoef = 1.0;
+    CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
+    long long nf = 9LL * (ctx->ixmax - 1) * (ctx->jymax - 1) * (ctx->kzmax - 1);
+    CK(cudaMemsetAsync(ctx->F, 0, nf * ctx->esz, ctx->st));
+    CK(cudaMemsetAsync(ctx->Gf, 0, nf * ctx->esz, ctx->st));
+    if (ctx->fp32)
+        CK(launch_states(dir, ctx->G, (const float *)vcur_ptr(ctx), (const float *)ctx->Vinit, ctx->d_sc,
+                         (float *)ctx->F, (float *)ctx->Gf, full_face_box(ctx), ctx->st));
+    else
+        CK(launch_states(dir, ctx->G, (const double *)vcur_ptr(ctx), (const double *)ctx->Vinit, ctx->d_sc,
+                         (double *)ctx->F, (double *)ctx->Gf, full_face_box(ctx), ctx->st));
+    int rc;
+    if ((rc = get_state(ctx, Vl, ctx->F, nf))) return rc;
+    if ((rc = get_state(ctx, Vr, ctx->Gf, nf))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return MHD_OK;
+}
+
+extern "C" int mhd_dbg_flux(mhd_ctx *ctx, int dir, double dt, double ch, double *Fo)
+{
+    if (!ctx || dir < 0 || dir > 2 || !Fo) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    ctx->h_sc->dt = dt;
+    ctx->h_sc->ch = ch;
+    ctx->h_sc->psicoef = 1.0;
+    CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
+    long long nf = 9LL * (ctx->ixmax - 1) * (ctx->jymax - 1) * (ctx->kzmax - 1);
+    CK(cudaMemsetAsync(ctx->F, 0, nf * ctx->esz, ctx->st));
+    if (ctx->fp32)
+        CK(launch_flux(dir, ctx->G, (const float *)vcur_ptr(ctx), (const float *)ctx->Vinit, ctx->d_sc,
+                       (float *)ctx->F, full_face_box(ctx), true, ctx->st));
+    else
+        CK(launch_flux(dir, ctx->G, (const double *)vcur_ptr(ctx), (const double *)ctx->Vinit, ctx->d_sc,
+                       (double *)ctx->F, full_face_box(ctx), true, ctx->st));
+    int rc = get_state(ctx, Fo, ctx->F, nf);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return MHD_OK;
+}
+
+extern "C" int mhd_dbg_source(mhd_ctx *ctx, double *S)
+{
+    if (!ctx || !S) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    double *d_S = NULL;
+    CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMallocAsync((void **)&d_S, 9 * ctx->nc * sizeof(double), ctx->st));
+    cudaError_t e = ctx->fp32 ? launch_source(ctx->G, (const float *)vcur_ptr(ctx), ctx->d_sc, ctx->d_trig, d_S,
+                                              ctx->st)
+                              : launch_source(ctx->G, (const double *)vcur_ptr(ctx), ctx->d_sc, ctx->d_trig,
+                                              d_S, ctx->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(S, d_S, 9 * ctx->nc * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+    cudaFreeAsync(d_S, ctx->st);
+    CK(e);
+    CK(cudaStreamSynchronize(ctx->st));
+    return MHD_OK;
+}
+
+extern "C" int mhd_dbg_gravity(mhd_ctx *ctx, double *gr)
+{
+    if (!ctx || !gr) return MHD_ERR_ARG;
+    double *d_g = NULL;
+    CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMallocAsync((void **)&d_g, 3 * ctx->nc * sizeof(double), ctx->st));
+    gravity_probe_kernel<<<(unsigned)((ctx->nc + 127) / 128), 128, 0, ctx->st>>>(ctx->G, ctx->d_sc, ctx->d_trig,
+                                                                                  d_g);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(gr, d_g, 3 * ctx->nc * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+    cudaFreeAsync(d_g, ctx->st);
+    CK(e);
+    CK(cudaStreamSynchronize(ctx->st));
+    return MHD_OK;
+}
+
+extern "C" int mhd_run(mhd_ctx *ctx, int nsteps, double *t)
+{
+    (void)nsteps; (void)t;
+    if (!ctx) return MHD_ERR_ARG;
+    return MHD_ERR_ARG;   /* device-resident stepping: not built yet */
+}
+
+extern "C" int mhd_diagnostics(mhd_ctx *ctx, mhd_diag *d)
+{
+    (void)d;
+    if (!ctx) return MHD_ERR_ARG;
+    return MHD_ERR_ARG;
+}

@@ -1,0 +1,463 @@
+/*
+ * mhd_kernels.cuh -- the step's kernels, templated on the real type T and
+ * instantiated once per precision form by mhd_fp64.cu / mhd_fp32.cu (which
+ * differ only in compile flags).
+ *
+ * One RK stage = flux(r) + flux(phi) + flux(z) + update + ghost:
+ *   flux    one thread per face the update reads; reconstruction of the two
+ *           adjacent cells, Riemann solver, GLM flux -> F/G/H[9][cells]
+ *   update  one thread per interior cell: sources, the stage's conservative
+ *           update, and -- because everything after it up to the next stage
+ *           is pointwise for interior cells -- the k=1 v_z zeroing (RK2), the
+ *           absorbing layers (last stage), UtoV and Check; the raw updated
+ *           state of the cells that boundary fills copy from is also kept
+ *   ghost   one thread per ghost cell: the reference's boundary-fill sequence
+ *           composed into one source cell and sign per ghost, then the same
+ *           pointwise tail as the interior.
+ */
+#ifndef MHD_KERNELS_CUH
+#define MHD_KERNELS_CUH
+
+#include "mhd_dev.cuh"
+#include "mhd_launch.h"
+
+namespace mhd {
+
+/* ------------------------------------------------------------------------ */
+/* fluxes                                                                    */
+/* ------------------------------------------------------------------------ */
+template <typename T, int DIR, bool REFLAYOUT>
+__global__ void __launch_bounds__(128)
+flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
+            T *__restrict__ F, Box b)
+{
+    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int nk = b.k1 - b.k0, nj = b.j1 - b.j0;
+    long long total = (long long)(b.i1 - b.i0) * nj * nk;
+    if (tid >= total) return;
+    int k = b.k0 + (int)(tid % nk);
+    long long r = tid / nk;
+    int j = b.j0 + (int)(r % nj);
+    int i = b.i0 + (int)(r / nj);
+    T dt = (T)sc->dt, ch = (T)sc->ch, psicoef = (T)sc->psicoef;
+    T L[9], R[9], Fo[9];
+    face_states<T, DIR>(G, V, Vinit, i, j, k, dt, psicoef, L, R);
+    face_flux<T, DIR>(G, L, R, i, ch, Fo);
+    if (REFLAYOUT) {
+        /* the reference's face layout [9][ixmax-1][jymax-1][kzmax-1] (probes) */
+        long long nf = (long long)(G.ixmax - 1) * (G.jymax - 1) * (G.kzmax - 1);
+        long long q = ((long long)i * (G.jymax - 1) + j) * (G.kzmax - 1) + k;
+#pragma unroll
+        for (int m = 0; m < 9; m++) F[m * nf + q] = Fo[m];
+    } else {
+        long long q = cidx(G, i, j, k);
+#pragma unroll
+        for (int m = 0; m < 9; m++) F[m * G.nc + q] = Fo[m];
+    }
+}
+
+/* reconstructed face states in the reference's face layout (probe) */
+template <typename T, int DIR>
+__global__ void __launch_bounds__(128)
+states_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
+              T *__restrict__ Vl, T *__restrict__ Vr, Box b)
+{
+    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int nk = b.k1 - b.k0, nj = b.j1 - b.j0;
+    long long total = (long long)(b.i1 - b.i0) * nj * nk;
+    if (tid >= total) return;
+    int k = b.k0 + (int)(tid % nk);
+    long long r = tid / nk;
+    int j = b.j0 + (int)(r % nj);
+    int i = b.i0 + (int)(r / nj);
+    T L[9], R[9];
+    face_states<T, DIR>(G, V, Vinit, i, j, k, (T)sc->dt, (T)sc->psicoef, L, R);
+    long long nf = (long long)(G.ixmax - 1) * (G.jymax - 1) * (G.kzmax - 1);
+    long long q = ((long long)i * (G.jymax - 1) + j) * (G.kzmax - 1) + k;
+#pragma unroll
+    for (int m = 0; m < 9; m++) { Vl[m * nf + q] = L[m]; Vr[m * nf + q] = R[m]; }
+}
+
+/* ------------------------------------------------------------------------ */
+/* update + pointwise tail                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* is cell (i,j,k) one that a boundary fill copies from? */
+__device__ __forceinline__ bool is_bc_source(const Geom &G, int i, int j, int k)
+{
+    return i == 1 || i == G.ixmax - 2 || j == 1 || j == G.jymax - 2 || k == 1 || k == 2 || k == G.kzmax - 2;
+}
+
+/* absorbing layers after the boundary fills of the last stage:
+ * XRightAbsorbBoundary (xboundary.h:133-138), CentralAbsorbBoundary
+ * (centralboundary.h:36-41), ZRightAbsorbBoundary (zboundary.h:40-46, RK2 only) */
+template <typename T>
+__device__ __forceinline__ void absorb(const Geom &G, const T *__restrict__ Uinit, int i, int j, int k, bool zright,
+                                      T u[9])
+{
+    const Tabs<T> &tb = tabs<T>(G);
+    long long q = cidx(G, i, j, k);
+    int ix0 = G.ixmax - 11, kz0 = G.kzmax - 11;
+    bool ax = i >= ix0, ac = i <= G.irin, az = zright && k >= kz0;
+    if (!(ax || ac || az)) return;
+    T fx = ax ? tb.xabs[i - ix0] : T(0), fc = ac ? tb.cabs[(long long)i * G.kzmax + k] : T(0);
+    T fz = az ? tb.zabs[k - kz0] : T(0);
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+        T ui = Uinit[m * G.nc + q];
+        T v = u[m];
+        if (ax) v -= (fx * (v - ui));
+        if (ac) v -= (fc * (v - ui));
+        if (az) v -= (fz * (v - ui));
+        u[m] = v;
+    }
+}
+
+/* kind: 0 U1=U-dtL (Halfstep/FirstStep), 1 U1=(3U+U1-dtL)/4 (SecondStep),
+ *       2 U=(U+2(U1-dtL))/3 (ThirdStep), 3 U=(U+U1-dtL)/2 (Fullstep) */
+template <typename T>
+__global__ void __launch_bounds__(128)
+update_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ F, const T *__restrict__ Gf,
+              const T *__restrict__ H, T *Un, T *U1, const T *__restrict__ Uinit,
+              const T *__restrict__ rhofloor, T *__restrict__ Vout, T *__restrict__ Uraw,
+              const StepScalars *__restrict__ sc, const double *__restrict__ trig, int kind, int last,
+              int *counters)
+{
+    if (sc->dtbad) return;
+    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int nk = G.kzmax - 2, nj = G.jymax - 2;
+    long long total = (long long)(G.ixmax - 2) * nj * nk;
+    int flags = 0;
+    if (tid < total) {
+        int k = 1 + (int)(tid % nk);
+        long long r = tid / nk;
+        int j = 1 + (int)(r % nj);
+        int i = 1 + (int)(r / nj);
+        const Tabs<T> &tb = tabs<T>(G);
+        const long long nc = G.nc, q = cidx(G, i, j, k);
+        const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
+        const long long gk = (long long)i * G.kzmax + k, pl = (long long)G.ixmax * G.kzmax;
+        const T g1 = tb.g[gk], g2 = tb.g[pl + gk], g3 = tb.g[2 * pl + gk];
+        const T g4 = tb.g[3 * pl + gk], g5 = tb.g[4 * pl + gk], g6 = tb.g[5 * pl + gk];
+        const T dt = (T)sc->dt, psicoef = (T)sc->psicoef;
+        T W[9], S[9], u[9];
+#pragma unroll
+        for (int m = 0; m < 9; m++) W[m] = V[m * nc + q];
+        source_at<T>(G, *sc, trig, i, j, k, W, S);
+#pragma unroll
+        for (int m = 0; m < 9; m++) {
+            const long long mq = m * nc + q;
+            T div = ((g2 * F[mq] - g1 * F[mq - si]) + (g4 * Gf[mq] - g3 * Gf[mq - sj]) + (g6 * H[mq] - g5 * H[mq - 1]));
+            T un = Un[mq], u1 = (kind == 0) ? T(0) : U1[mq];
+            if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
+            T v;
+            if (kind == 0) v = un - dt * div + dt * S[m];
+            else if (kind == 1) v = T(0.25) * (T(3.0) * un + u1 - dt * div + dt * S[m]);
+            else if (kind == 2) v = T(MHD_ONEO3) * (un + T(2.0) * (u1 - dt * div + dt * S[m]));
+            else v = T(0.5) * (un + u1 - dt * div + dt * S[m]);
+            u[m] = v;
+        }
+        if (is_bc_source(G, i, j, k)) {
+#pragma unroll
+            for (int m = 0; m < 9; m++) Uraw[m * nc + q] = u[m];
+        }
+        if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);   /* zboundary.h:87 */
+        if (last) absorb<T>(G, Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
+        flags = utov_check<T>(G, i, rhofloor[q], u, W);
+        T *Uo = (kind == 0 || kind == 1) ? U1 : Un;
+#pragma unroll
+        for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; Vout[m * nc + q] = W[m]; }
+    }
+    add_counters(flags, counters);
+}
+
+/* Ghost cell -> (source interior cell, sign flip mask) after the fill sequence
+ * Y periodic (yboundary.h:97-154), X axis (xboundary.h:33-72), X right free
+ * (xboundary.h:322-346), then Z: RK2 k=0 antisymmetric in v_z and k=kzmax-1
+ * free (zboundary.h:67-96,203-226); RK3 periodic (zboundary.h:105-161).
+ * Later fills win, so the map is applied Z first, then X, then Y. */
+__device__ __forceinline__ void ghost_source(const Geom &G, int i, int j, int k, int &si, int &sj, int &sk,
+                                             unsigned &neg)
+{
+    neg = 0u;
+    sk = k;
+    if (G.scheme == MHD_SCHEME_RK2) {
+        if (k == 0) { sk = 2; neg ^= 1u << 3; }
+        else if (k == G.kzmax - 1) sk = G.kzmax - 2;
+    } else {
+        if (k == 0) sk = G.kzmax - 2;
+        else if (k == G.kzmax - 1) sk = 1;
+    }
+    si = i; sj = j;
+    int half = G.jy / 2;
+    if (i == 0) {
+        si = 1;
+        sj = (j < half + 1) ? j + half : j - half;
+        neg ^= (1u << 1) | (1u << 2) | (1u << 4) | (1u << 5);
+        return;   /* the axis source row j' is always interior */
+    }
+    if (i == G.ixmax - 1) si = G.ixmax - 2;
+    if (j == 0) sj = G.jymax - 2;
+    else if (j == G.jymax - 1) sj = 1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+ghost_kernel(Geom G, const T *__restrict__ Uraw, T *Uo, const T *__restrict__ Uinit,
+             const T *__restrict__ rhofloor, T *__restrict__ Vout, const StepScalars *__restrict__ sc,
+             int last, int *counters)
+{
+    if (sc->dtbad) return;
+    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
+    const long long nkplane = 2 * ni * nj;
+    const long long njplane = 2 * ni * (nk - 2);
+    const long long niplane = 2 * (nj - 2) * (nk - 2);
+    int flags = 0;
+    if (tid < nkplane + njplane + niplane) {
+        int i, j, k;
+        if (tid < nkplane) {
+            k = (tid < ni * nj) ? 0 : (int)nk - 1;
+            long long r = tid % (ni * nj);
+            i = (int)(r / nj); j = (int)(r % nj);
+        } else if (tid < nkplane + njplane) {
+            long long r = tid - nkplane;
+            j = (r < ni * (nk - 2)) ? 0 : (int)nj - 1;
+            r %= ni * (nk - 2);
+            i = (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
+        } else {
+            long long r = tid - nkplane - njplane;
+            i = (r < (nj - 2) * (nk - 2)) ? 0 : (int)ni - 1;
+            r %= (nj - 2) * (nk - 2);
+            j = 1 + (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
+        }
+        int si, sj, sk;
+        unsigned neg;
+        ghost_source(G, i, j, k, si, sj, sk, neg);
+        const long long nc = G.nc, q = cidx(G, i, j, k), qs = cidx(G, si, sj, sk);
+        T u[9], W[9];
+#pragma unroll
+        for (int m = 0; m < 9; m++) {
+            T v = Uraw[m * nc + qs];
+            u[m] = ((neg >> m) & 1u) ? -v : v;
+        }
+        if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);
+        if (last) absorb<T>(G, Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
+        flags = utov_check<T>(G, i, rhofloor[q], u, W);
+#pragma unroll
+        for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; Vout[m * nc + q] = W[m]; }
+    }
+    add_counters(flags, counters);
+}
+
+/* ------------------------------------------------------------------------ */
+/* CFL reduction (setdt.h:33-89), always FP64                                */
+/* ------------------------------------------------------------------------ */
+__device__ __forceinline__ MaxLoc better(MaxLoc a, MaxLoc b)
+{
+    /* larger value wins; equal values: the smaller cell index (the serial
+     * reference keeps the first cell reaching the maximum: strict '>') */
+    if (b.q < 0) return a;
+    if (a.q < 0) return b;
+    if (b.v > a.v || (b.v == a.v && b.q < a.q)) return b;
+    return a;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+setdt_kernel(Geom G, const T *__restrict__ V, MaxLoc *part)
+{
+    __shared__ MaxLoc sm[8];
+    const int ilo = 1, ihi = G.ixmax - 1 - 10;
+    const long long nk = G.kzmax - 2, nj = G.jymax - 2;
+    const long long total = (long long)(ihi - ilo) * nj * nk;
+    MaxLoc best = {0.0, -1};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        int k = 1 + (int)(t % nk);
+        long long r = t / nk;
+        int j = 1 + (int)(r % nj);
+        int i = ilo + (int)(r / nj);
+        const long long nc = G.nc, q = cidx(G, i, j, k);
+        double v0 = V[q], v1 = V[nc + q], v2v = V[2 * nc + q], v3 = V[3 * nc + q];
+        double v4 = V[4 * nc + q], v5 = V[5 * nc + q], v6 = V[6 * nc + q], v7 = V[7 * nc + q];
+        double v2 = v1 * v1 + v2v * v2v + v3 * v3;
+        double b2 = v4 * v4 + v5 * v5 + v6 * v6;
+        double t1 = sqrt(v2 + (MHD_GM * v7 + b2) / v0) / G.minlength[(long long)i * G.kzmax + k];
+        int cl = G.cooling ? cooling_rate(v0, v7) : 0;
+        double tc = (2.0 * ((v0 * v0 * cl) / (1.5 * v7)));
+        double tmp = rmax<double>(t1, tc);
+        /* the reference only takes a cell when tmp > running max (from 0) */
+        if (tmp > best.v || (best.q >= 0 && tmp == best.v && q < best.q)) {
+            if (tmp > 0.0) { best.v = tmp; best.q = q; }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        MaxLoc other;
+        other.v = __shfl_down_sync(0xffffffffu, best.v, o);
+        other.q = __shfl_down_sync(0xffffffffu, best.q, o);
+        best = better(best, other);
+    }
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        MaxLoc b = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = better(b, sm[w]);
+        part[blockIdx.x] = b;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* conversions                                                               */
+/* ------------------------------------------------------------------------ */
+template <typename T>
+__global__ void cvt_from_f64(const double *__restrict__ src, T *__restrict__ dst, long long n)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[t] = (T)src[t];
+}
+
+template <typename T>
+__global__ void cvt_to_f64(const T *__restrict__ src, double *__restrict__ dst, long long n)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[t] = (double)src[t];
+}
+
+/* source term probe (SpiralGravityCooling over all cells) */
+template <typename T>
+__global__ void source_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc,
+                              const double *__restrict__ trig, double *__restrict__ S)
+{
+    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= G.nc) return;
+    int k = (int)(tid % G.kzmax);
+    long long r = tid / G.kzmax;
+    int j = (int)(r % G.jymax);
+    int i = (int)(r / G.jymax);
+    T W[9], Sv[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) W[m] = V[m * G.nc + tid];
+    source_at<T>(G, *sc, trig, i, j, k, W, Sv);
+#pragma unroll
+    for (int m = 0; m < 9; m++) S[m * G.nc + tid] = (double)Sv[m];
+}
+
+/* ------------------------------------------------------------------------ */
+/* launchers                                                                 */
+/* ------------------------------------------------------------------------ */
+static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <typename T>
+cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,
+                          Box b, bool reflayout, cudaStream_t st)
+{
+    long long n = (long long)(b.i1 - b.i0) * (b.j1 - b.j0) * (b.k1 - b.k0);
+    if (n <= 0) return cudaSuccess;
+    unsigned nb = nblocks(n, 128);
+#define MHD_FLUX_CASE(D, RL) flux_kernel<T, D, RL><<<nb, 128, 0, st>>>(G, V, Vinit, sc, F, b)
+    if (reflayout) {
+        if (dir == 0) MHD_FLUX_CASE(0, true); else if (dir == 1) MHD_FLUX_CASE(1, true); else MHD_FLUX_CASE(2, true);
+    } else {
+        if (dir == 0) MHD_FLUX_CASE(0, false); else if (dir == 1) MHD_FLUX_CASE(1, false); else MHD_FLUX_CASE(2, false);
+    }
+#undef MHD_FLUX_CASE
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_states_t(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *Vl,
+                            T *Vr, Box b, cudaStream_t st)
+{
+    long long n = (long long)(b.i1 - b.i0) * (b.j1 - b.j0) * (b.k1 - b.k0);
+    if (n <= 0) return cudaSuccess;
+    unsigned nb = nblocks(n, 128);
+    if (dir == 0) states_kernel<T, 0><<<nb, 128, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
+    else if (dir == 1) states_kernel<T, 1><<<nb, 128, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
+    else states_kernel<T, 2><<<nb, 128, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_update_t(const Geom &G, const StageArgs<T> &a, cudaStream_t st)
+{
+    long long n = (long long)(G.ixmax - 2) * (G.jymax - 2) * (G.kzmax - 2);
+    update_kernel<T><<<nblocks(n, 128), 128, 0, st>>>(G, a.V, a.F, a.G, a.H, a.Un, a.U1, a.Uinit, a.rhofloor,
+                                                      a.Vout, a.Uraw, a.sc, a.trig, a.kind, a.last, a.counters);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    long long ng = 2LL * G.ixmax * G.jymax + 2LL * G.ixmax * (G.kzmax - 2) + 2LL * (G.jymax - 2) * (G.kzmax - 2);
+    T *Uo = (a.kind == 0 || a.kind == 1) ? a.U1 : a.Un;
+    ghost_kernel<T><<<nblocks(ng, 128), 128, 0, st>>>(G, a.Uraw, Uo, a.Uinit, a.rhofloor, a.Vout, a.sc, a.last,
+                                                      a.counters);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_setdt_t(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st)
+{
+    setdt_kernel<T><<<nblk, 256, 0, st>>>(G, V, part);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_source_t(const Geom &G, const T *V, const StepScalars *sc, const double *trig, double *S,
+                            cudaStream_t st)
+{
+    source_kernel<T><<<nblocks(G.nc, 128), 128, 0, st>>>(G, V, sc, trig, S);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_cvt_t(const double *src, T *dst, long long n, cudaStream_t st)
+{
+    cvt_from_f64<T><<<1024, 256, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream_t st)
+{
+    cvt_to_f64<T><<<1024, 256, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+} /* namespace mhd */
+
+/* explicit overloads for one T, expanded by the instantiating .cu file */
+#define MHD_DEFINE_LAUNCHERS(T)                                                                              \
+    namespace mhd {                                                                                          \
+    cudaError_t launch_flux(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, \
+                            Box b, bool reflayout, cudaStream_t st)                                          \
+    {                                                                                                        \
+        return launch_flux_t<T>(dir, G, V, Vinit, sc, F, b, reflayout, st);                                  \
+    }                                                                                                        \
+    cudaError_t launch_states(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,     \
+                              T *Vl, T *Vr, Box b, cudaStream_t st)                                          \
+    {                                                                                                        \
+        return launch_states_t<T>(dir, G, V, Vinit, sc, Vl, Vr, b, st);                                      \
+    }                                                                                                        \
+    cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st)                          \
+    {                                                                                                        \
+        return launch_update_t<T>(G, a, st);                                                                 \
+    }                                                                                                        \
+    cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st)            \
+    {                                                                                                        \
+        return launch_setdt_t<T>(G, V, part, nblk, st);                                                      \
+    }                                                                                                        \
+    cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
+                              double *S, cudaStream_t st)                                                    \
+    {                                                                                                        \
+        return launch_source_t<T>(G, V, sc, trig, S, st);                                                    \
+    }                                                                                                        \
+    cudaError_t launch_cvt(const double *src, T *dst, long long n, cudaStream_t st)                          \
+    {                                                                                                        \
+        return launch_cvt_t<T>(src, dst, n, st);                                                             \
+    }                                                                                                        \
+    cudaError_t launch_cvt_back(const T *src, double *dst, long long n, cudaStream_t st)                     \
+    {                                                                                                        \
+        return launch_cvt_back_t<T>(src, dst, n, st);                                                        \
+    }                                                                                                        \
+    }
+
+#endif

@@ -1,0 +1,53 @@
+/*
+ * mhd_launch.h -- launcher interface between the context code (mhd_ctx.cu)
+ * and the per-precision kernel translation units (mhd_fp64.cu, mhd_fp32.cu).
+ * Overloaded on the state type: double = plain form, float = precision form.
+ */
+#ifndef MHD_LAUNCH_H
+#define MHD_LAUNCH_H
+
+#include "mhd_dev.cuh"
+
+namespace mhd {
+
+/* half-open index box [i0,i1) x [j0,j1) x [k0,k1) */
+struct Box {
+    int i0, i1, j0, j1, k0, k1;
+};
+
+struct MaxLoc {
+    double v;
+    long long q;
+};
+
+template <typename T>
+struct StageArgs {
+    const T *V;            /* stage input primitives */
+    const T *F, *G, *H;    /* fluxes */
+    T *Un, *U1;            /* U^n and U^(1) (or U^(2)); output goes to one of them */
+    const T *Uinit, *rhofloor;
+    T *Vout, *Uraw;
+    const StepScalars *sc;
+    const double *trig;
+    int kind, last;
+    int *counters;
+};
+
+#define MHD_DECLARE_LAUNCHERS(T)                                                                             \
+    cudaError_t launch_flux(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, \
+                            Box b, bool reflayout, cudaStream_t st);                                         \
+    cudaError_t launch_states(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,     \
+                              T *Vl, T *Vr, Box b, cudaStream_t st);                                         \
+    cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                        \
+    cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st);            \
+    cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
+                              double *S, cudaStream_t st);                                                   \
+    cudaError_t launch_cvt(const double *src, T *dst, long long n, cudaStream_t st);                         \
+    cudaError_t launch_cvt_back(const T *src, double *dst, long long n, cudaStream_t st);
+
+MHD_DECLARE_LAUNCHERS(double)
+MHD_DECLARE_LAUNCHERS(float)
+
+} /* namespace mhd */
+
+#endif

@@ -1,0 +1,202 @@
+/*
+ * mhd_gpu.h -- C-ABI of libmhdgpu.so, the GB300 (sm_103a) implementation of
+ * the cylindrical (r, phi, z) GLM-MHD TVD Runge-Kutta step of
+ * github-nakasho/171026-1-3dhlld-cyli-gal.
+ *
+ * The reference is one C program whose step loop (main.c:316-393) calls three
+ * functions on global arrays:
+ *
+ *     Setdt();          setdt.h:24       -> mhd_setdt()
+ *     SpiralGravity();  spiralgravity.h:20 -> mhd_spiral_gravity()
+ *     TVDRK();          tvdrungekutta.h:16 -> mhd_tvdrk()
+ *
+ * and stops the program on a bad dt (main.c:331-334) -> mhd_step() returns
+ * MHD_ERR_DT instead.  A reference host keeps its globals, array layout
+ * ([m][i][j][k], k fastest, FP64, one ghost cell per side) and file formats;
+ * it hands its arrays to mhd_create()/mhd_upload() once and calls the step
+ * functions in place of its own.  INTEGRATION.md shows the calls.
+ *
+ * Conventions: every function returns 0 (MHD_OK) or a negative MHD_ERR_*
+ * code; nothing prints or exits.  A context is used by one host thread at a
+ * time and owns one CUDA stream.  The library copies every host array it is
+ * given; the caller keeps ownership.
+ */
+#ifndef MHD_GPU_H
+#define MHD_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ------------------------------------------------------ */
+#define MHD_OK 0
+#define MHD_ERR_ARG (-1)      /* bad argument, shape or unsupported option */
+#define MHD_ERR_CUDA (-2)     /* CUDA runtime error */
+#define MHD_ERR_DT (-3)       /* dt = inf or dt < dtmin (main.c:331) */
+#define MHD_ERR_NOMEM (-4)    /* host or device allocation failed */
+#define MHD_ERR_STATE (-5)    /* call out of order (e.g. step before upload) */
+#define MHD_ERR_TIMEOUT (-6)  /* a bounded device-side wait gave up */
+#define MHD_ERR_NODEV (-7)    /* no CUDA device */
+#define MHD_ERR_IO (-8)       /* file read/write failed (host I/O helpers) */
+
+/* ---- scheme choices ---------------------------------------------------- */
+#define MHD_LIMITER_MINMOD 0  /* MinmodLimiterX/Y/Z (limiterx.h:32, limitery.h:33, limiterz.h:30) */
+#define MHD_LIMITER_MC 1      /* MCLimiterX/Y/Z (limiterx.h:335, limitery.h:197, limiterz.h:294) */
+#define MHD_SOLVER_HLLD 0     /* HLLDX/Y/Z (hlldx.h:28, hlldy.h:30, hlldz.h:28) */
+#define MHD_SOLVER_HLL 1      /* HLLX/Y/Z (hllx.h:29, hlly.h:29, hllz.h:26) */
+#define MHD_SCHEME_RK2 2      /* live TVDRK: Halfstep + Fullstep (tvdrungekutta.h:31-41) */
+#define MHD_SCHEME_RK3 3      /* FirstStep/SecondStep/ThirdStep (tvdrungekutta.h:56-83) */
+#define MHD_PREC_FP64 0       /* plain FP64: bit-identical to the reference C */
+#define MHD_PREC_FP32 1       /* FP32 state and fluxes, FP64 repair of the fragile steps */
+
+/* Physics and scheme knobs.  Reference: input.h:58-96 (#defines and globals),
+ * constant.h:62-79.  gamma=5/3 and cr=0.18 are fixed as in constant.h. */
+typedef struct {
+    double cfl, dtmin, rhocr, prcr, betacr;
+    double epssp0, tausp, scalez, scaler, scalephase;
+    int armnum;
+    double omegasp, omegapattern, pitch;
+    int limiter;    /* MHD_LIMITER_* */
+    int solver;     /* MHD_SOLVER_* */
+    int scheme;     /* MHD_SCHEME_* */
+    int cooling;    /* 0 off, 1 Cooling() of cooling.h:22 */
+    int gravity;    /* 0 off, 1 Gr*axi + SpiralGravity() each step */
+    int precision;  /* MHD_PREC_* */
+} mhd_params;
+
+/* Grid construction parameters (input.h:45-76). */
+typedef struct {
+    int ix, jy, kz;                   /* interior cells in r, phi, z (jy even) */
+    double x0, dx0, lx;               /* first interior r centre, r spacing, stretch start */
+    double y0, ly;                    /* first interior phi centre, phi extent */
+    double z0, dz0, lz;               /* first interior z centre, z spacing, stretch start */
+    double stretchratio, dxmax, dzmax;
+    double rin;                       /* central absorbing radius */
+} mhd_gridspec;
+
+/* The reference's grid globals (commongrid.h:42-62, commontemp.h:320-322,
+ * commonfield.h:130-132), by host pointer in the reference's own layout.
+ * ixmax = ix+2 etc.; face-shaped arrays are [ixmax-1][jymax-1][kzmax-1]. */
+typedef struct {
+    int ix, jy, kz, irin;
+    int compact;        /* 0: the reference's 3D layouts below; 1: the j-independent
+                           tables g1..g6, minlength, Gr*axi given once per (i,k):
+                           g* as [ixmax-1][kzmax-1], the others as [ixmax][kzmax] */
+    double dx0, rin;
+    const double *x, *xm, *dx, *dxm, *oneox, *oneodx;   /* [ixmax] */
+    const double *y;                                     /* [jymax] */
+    double dy, oneody;
+    const double *z, *zm, *dz, *dzm, *oneodz;           /* [kzmax] */
+    const double *g1, *g2, *g3, *g4, *g5, *g6;          /* face-shaped, j-independent */
+    const double *minlength;                             /* [ixmax][jymax][kzmax], j-independent */
+    double minminlength;
+    const double *x_absorb_factor;                       /* [11] */
+    const double *z_absorb_factor;                       /* [11] */
+    const double *c_absorb_factor;                       /* [irin+1][kzmax] */
+    const double *Grxaxi, *Gryaxi, *Grzaxi;              /* [ixmax][jymax][kzmax], j-independent,
+                                                            or NULL for zero */
+} mhd_grid;
+
+/* Totals over the interior cells, each weighted by the cell volume
+ * 0.5*(xm[i]^2-xm[i-1]^2)*dy*dzm[k-1] (cylindricalgrid.h:114), summed in FP64:
+ * mass = sum rho dV, angmom = sum (r rho v_phi) dV, energy = sum E dV,
+ * psi = sum |psi| dV; maxdivb = max |div B| with central differences
+ * (1/r) d(r B_r)/dr + (1/r) dB_phi/dphi + dB_z/dz at interior cells. */
+typedef struct {
+    double mass, angmom, energy, psi, maxdivb;
+} mhd_diag;
+
+typedef struct mhd_ctx mhd_ctx;
+
+/* ---- host helpers (no GPU) ---------------------------------------------- */
+const char *mhd_errstr(int code);
+void mhd_params_default(mhd_params *p);       /* reference values (input.h, constant.h) */
+int mhd_gridspec_disc(int nr, int nphi, int nz, mhd_gridspec *out); /* r in [0.1,1.5], z in [-0.5,0.5] */
+int mhd_gridspec_shipped(mhd_gridspec *out);  /* input.h:45-76: 240x64x200 stretched */
+/* Doubles of storage mhd_grid_build() needs for the tables. */
+size_t mhd_grid_storage(const mhd_gridspec *gs);
+/* CylindricalGrid() (cylindricalgrid.h:25-227): fills caller storage and
+ * points g's members into it, with compact=1 tables.  Gr*axi are set to NULL. */
+int mhd_grid_build(const mhd_gridspec *gs, double *storage, mhd_grid *g);
+/* InitialGravity() (initialgravity.h:22-79) into three arrays shaped like
+ * g's minlength ([ixmax][kzmax] when compact, else cell-shaped). */
+int mhd_initial_gravity(const mhd_grid *g, double *grxaxi, double *gryaxi, double *grzaxi);
+/* Project initial condition (no counterpart in the reference): isothermal
+ * rotating disc rho = exp(-z^2/(2*0.1^2)) + 1e-3, p = 0.01 rho, v_phi = 1,
+ * B_phi = sqrt(2p/beta), with a seeded uniform perturbation of amplitude amp
+ * (rho *= 1+amp*u, v += amp*u, u in [-1,1) from splitmix64(seed)).  Writes V,
+ * U (VtoU, vtou.h:20-62), Uinit=U, Vinit=V, rhofloor=rhocr*rho
+ * (SaveInitial, saveinitial.h:18-50).  Any output pointer may be NULL. */
+int mhd_ic_disc(const mhd_grid *g, double beta, double amp, unsigned long long seed,
+                double rhocr, double *U, double *V, double *Uinit, double *Vinit,
+                double *rhofloor);
+/* VtoU() (vtou.h:20-62) on caller arrays. */
+int mhd_vtou(const mhd_grid *g, const double *V, double *U);
+
+/* ---- device context: the step ------------------------------------------- */
+int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out);
+void mhd_destroy(mhd_ctx *ctx);
+/* State upload, host layout [9][ixmax][jymax][kzmax] FP64 (commonfield.h:114,
+ * commontemp.h:305-308).  Uinit/Vinit/rhofloor feed the absorbing layers, the
+ * MC z boundary and the density floor; NULL means "same as U", "same as V"
+ * and rhocr*U[0] (SaveInitial, saveinitial.h:34-40) respectively. */
+int mhd_upload(mhd_ctx *ctx, const double *U, const double *V, const double *Uinit,
+               const double *Vinit, const double *rhofloor);
+int mhd_download(mhd_ctx *ctx, double *U, double *V);
+/* Setdt (setdt.h:24-94): dt = cfl/max, ch = minminlength*max; ijk = the
+ * first cell (in i,j,k order) attaining the max, as the serial reference. */
+int mhd_setdt(mhd_ctx *ctx, double *dt, double *ch, int ijk[3]);
+/* SpiralGravity (spiralgravity.h:20-124) at time t: takes effect for the
+ * following mhd_tvdrk(). */
+int mhd_spiral_gravity(mhd_ctx *ctx, double t);
+/* TVDRK (tvdrungekutta.h:16-78) with the given dt and ch; counters = the
+ * density, pressure and beta floor counts of the last stage's Check
+ * (check.h:180-183). */
+int mhd_tvdrk(mhd_ctx *ctx, double dt, double ch, int counters[3]);
+/* One pass of main.c:319-351: Setdt, dt guard, SpiralGravity (if gravity),
+ * TVDRK, t += dt.  Returns MHD_ERR_DT (state untouched) where the reference
+ * exits. */
+int mhd_step(mhd_ctx *ctx, double *t, double *dt, double *ch, int counters[3]);
+/* nsteps of mhd_step with no host round trip: dt, ch and the psi factor stay
+ * on the device and the whole step is one CUDA graph launch.  Only for
+ * MHD_PREC_FP32 (the plain form computes exp() on the host for bitwise
+ * parity).  *t advances by the sum of the dt's. */
+int mhd_run(mhd_ctx *ctx, int nsteps, double *t);
+int mhd_diagnostics(mhd_ctx *ctx, mhd_diag *d);
+/* The CUDA stream the context launches on (as a cudaStream_t). */
+void *mhd_stream(mhd_ctx *ctx);
+
+/* ---- per-kernel probes (parity tests) ------------------------------------ */
+/* Reconstructed face states of one direction (dir 0 r, 1 phi, 2 z) with the
+ * given dt, in the reference's face layout [9][ixmax-1][jymax-1][kzmax-1];
+ * entries the step never reads are left zero. */
+int mhd_dbg_limiter(mhd_ctx *ctx, int dir, double dt, double *Vl, double *Vr);
+/* Riemann flux + GLM flux of one direction (F, G or H) in the face layout. */
+int mhd_dbg_flux(mhd_ctx *ctx, int dir, double dt, double ch, double *F);
+/* SpiralGravityCooling source S (source.h:26-134), cell layout [9][...]. */
+int mhd_dbg_source(mhd_ctx *ctx, double *S);
+/* Grx, Gry, Grz of the last mhd_spiral_gravity(), cell layout [3][...]. */
+int mhd_dbg_gravity(mhd_ctx *ctx, double *gr);
+
+/* ---- batched form: many independent discs ------------------------------- */
+typedef struct mhd_batch mhd_batch;
+int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *params, mhd_batch **out);
+void mhd_batch_destroy(mhd_batch *b);
+int mhd_batch_upload(mhd_batch *b, int disc, const double *U, const double *V,
+                     const double *Uinit, const double *Vinit, const double *rhofloor);
+int mhd_batch_download(mhd_batch *b, int disc, double *U, double *V);
+/* nsteps steps of every disc, each with its own dt; t[n] advance in place;
+ * status[n] = 0 or MHD_ERR_DT for a disc whose dt guard fired (that disc then
+ * stops advancing).  One persistent launch per RK stage, the whole step
+ * captured as a CUDA graph. */
+int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status);
+/* Times candidate tile shapes on the current state and keeps the fastest;
+ * the state is restored afterwards.  best[4] = {tile_i, tile_j, tile_k, threads}. */
+int mhd_batch_tune(mhd_batch *b, int *best);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

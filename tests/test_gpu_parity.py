@@ -1,0 +1,143 @@
+"""GPU parity: the CUDA library (through its C-ABI) against the oracle on the
+same seeded inputs.
+
+Plain FP64 form: bit-identical (np.array_equal, NaN positions included) for
+every per-kernel probe and for whole steps -- the reference is FP64 C without
+contraction and the kernels are compiled --fmad=false with IEEE div/sqrt.
+Precision form: per-variable relative L1 against the FP64 oracle, tolerance
+written in the test.
+"""
+import numpy as np
+import pytest
+
+from mhdcase import VARIANTS, make_case, oracle_for, rel_l1, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+SMALL = (16, 16, 16)
+ODD = (20, 12, 14)
+
+
+def same(a, b):
+    return np.array_equal(a, b, equal_nan=True)
+
+
+def describe(a, b):
+    d = np.abs(a - b)
+    idx = np.unravel_index(np.nanargmax(d), d.shape) if np.isfinite(d).any() else None
+    return "max|diff|=%g at %s (a=%r b=%r)" % (np.nanmax(d), idx, a[idx] if idx else None, b[idx] if idx else None)
+
+
+@pytest.mark.parametrize("variant", ["rk3_minmod_hlld", "rk3_mc_hlld_grav_cool", "rk3_minmod_hll"])
+@pytest.mark.parametrize("dims", [SMALL, ODD])
+def test_probes_bitwise(M, P, variant, dims):
+    grid, params, U, V = make_case(M, variant, dims)
+    o = oracle_for(M, P, grid, params)
+    o.load(U, V)
+    d = M.Disc(grid, params)
+    d.upload(U, V)
+    # Setdt (setdt.h:24-94)
+    dt_o, ch_o, ijk_o = o.setdt()
+    dt_g, ch_g, ijk_g = d.setdt()
+    assert dt_o == dt_g and ch_o == ch_g and ijk_o == ijk_g
+    # reconstruction + Riemann fluxes per direction
+    o.set_dtch(dt_o, ch_o)
+    for dr in range(3):
+        Vl_o, Vr_o = o.limiter(dr)
+        Vl_g, Vr_g = d.limiter(dr, dt_o)
+        assert same(Vl_o, Vl_g), "Vl dir %d: %s" % (dr, describe(Vl_o, Vl_g))
+        assert same(Vr_o, Vr_g), "Vr dir %d: %s" % (dr, describe(Vr_o, Vr_g))
+        F_o = o.flux(dr)
+        F_g = d.flux(dr, dt_o, ch_o)
+        assert same(F_o, F_g), "flux dir %d: %s" % (dr, describe(F_o, F_g))
+    # gravity and sources at a time inside the spiral ramp
+    t = 0.37
+    if params.gravity:
+        # SpiralGravity runs only when gravity is on (mhd_spiral_gravity is a
+        # no-op otherwise, Grx..Grz stay zero as in a reference run without it)
+        o.spiral(t)
+        d.spiral(t)
+        _, gr_o = o.gravity()
+        gr_g = d.gravity()
+        assert same(gr_o, gr_g), describe(gr_o, gr_g)
+    S_o = o.source()
+    S_g = d.source()
+    assert same(S_o, S_g), describe(S_o, S_g)
+    d.close()
+    o.close()
+
+
+@pytest.mark.parametrize("variant", sorted(VARIANTS))
+def test_steps_bitwise(M, P, variant):
+    nsteps = 10
+    grid, params, U, V = make_case(M, variant, SMALL)
+    o = oracle_for(M, P, grid, params)
+    Uo, Vo, log, t_o = run_oracle(o, U, V, nsteps)
+    d = M.Disc(grid, params)
+    d.upload(U, V)
+    t = 0.0
+    for n in range(nsteps):
+        rc, t, dt, ch, cnt = d.step(t)
+        assert rc == 0
+        assert (dt, ch) == log[n][:2], "step %d dt/ch" % n
+        assert tuple(int(c) for c in cnt) == log[n][2], "step %d floor counters" % n
+    Ug, Vg = d.download()
+    assert t == t_o
+    assert same(Uo, Ug), describe(Uo, Ug)
+    assert same(Vo, Vg), describe(Vo, Vg)
+    d.close()
+    o.close()
+
+
+def test_disc1_64x64x32_ten_steps(M, P):
+    """The CPU-runnable reference case: 64x64x32, 10 RK3 steps, all 9
+    conserved variables; bit-identical (so well inside 1e-12 relative L1)."""
+    grid, params, U, V = make_case(M, "rk3_minmod_hlld", (64, 64, 32))
+    o = oracle_for(M, P, grid, params)
+    Uo, Vo, log, _ = run_oracle(o, U, V, 10)
+    d = M.Disc(grid, params)
+    d.upload(U, V)
+    t = 0.0
+    for n in range(10):
+        rc, t, dt, ch, cnt = d.step(t)
+        assert rc == 0 and dt == log[n][0]
+    Ug, Vg = d.download()
+    assert rel_l1(Ug, Uo).max() <= 1e-12
+    assert same(Uo, Ug), describe(Uo, Ug)
+    d.close()
+    o.close()
+
+
+def test_dt_guard(M):
+    """main.c:331: dt < dtmin stops the run -- here MHD_ERR_DT, state untouched."""
+    grid, params, U, V = make_case(M, "rk3_minmod_hlld", SMALL, dtmin=1.0e3)
+    d = M.Disc(grid, params)
+    d.upload(U, V)
+    rc, t, dt, ch, cnt = d.step(0.0)
+    assert rc == M.MHD_ERR_DT and t == 0.0
+    U2, V2 = d.download()
+    assert same(U, U2) and same(V, V2)
+    d.close()
+
+
+def test_precision_form_against_fp64(M, P):
+    """FP32 state/fluxes with FP64 repair vs the FP64 oracle after 10 steps:
+    every conserved variable within 1e-4 relative L1 on this small grid."""
+    grid, params, U, V = make_case(M, "rk3_minmod_hlld", (32, 32, 32))
+    o = oracle_for(M, P, grid, params)
+    Uo, Vo, _, _ = run_oracle(o, U, V, 10)
+    params32 = M.default_params(**{k: v for k, v in params.as_dict().items() if k != "precision"},
+                                precision="fp32")
+    d = M.Disc(grid, params32)
+    d.upload(U, V)
+    t = 0.0
+    for _ in range(10):
+        rc, t, dt, ch, cnt = d.step(t)
+        assert rc == 0
+    Ug, Vg = d.download()
+    err = rel_l1(Ug, Uo)
+    # psi starts at 0 and stays tiny: judge it against the field scale instead
+    err[8] = np.abs(Ug[8] - Uo[8]).sum() / max(np.abs(Uo[4:7]).sum(), 1e-300)
+    assert np.all(err[:8] < 1e-4), err
+    d.close()
+    o.close()
