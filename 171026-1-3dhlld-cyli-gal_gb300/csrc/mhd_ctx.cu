@@ -54,7 +54,64 @@ struct mhd_ctx {
     cudaGraphExec_t gexec;
     int graph_ready;
     int *d_cnt_run;
+    /* instrumentation */
+    long long launches;
+    int prof, nslot;
+    cudaEvent_t ev[2 * 256];
+    int slot_kind[256];
+    double prof_ms[MHD_PROF_NKIND];
+    long long prof_n[MHD_PROF_NKIND];
+    cudaEvent_t tev[2];
 };
+
+enum { PK_FLUX_R = 0, PK_FLUX_PHI = 1, PK_FLUX_Z = 2, PK_UPDATE = 3, PK_GHOST = 4, PK_SETDT = 5, PK_TRIG = 6,
+       PK_CVT = 7 };
+static const int MAXSLOT = 256;
+
+/* fold the recorded event pairs into the per-kind totals */
+static cudaError_t prof_harvest(mhd_ctx *ctx)
+{
+    if (ctx->nslot == 0) return cudaSuccess;
+    cudaError_t e = cudaEventSynchronize(ctx->ev[2 * ctx->nslot - 1]);
+    if (e != cudaSuccess) return e;
+    for (int s = 0; s < ctx->nslot; s++) {
+        float ms = 0.f;
+        e = cudaEventElapsedTime(&ms, ctx->ev[2 * s], ctx->ev[2 * s + 1]);
+        if (e != cudaSuccess) return e;
+        ctx->prof_ms[ctx->slot_kind[s]] += ms;
+        ctx->prof_n[ctx->slot_kind[s]] += 1;
+    }
+    ctx->nslot = 0;
+    return cudaSuccess;
+}
+
+static cudaError_t prof_begin(mhd_ctx *ctx, int kind)
+{
+    if (!ctx->prof) return cudaSuccess;
+    if (ctx->nslot == MAXSLOT) {
+        cudaError_t e = prof_harvest(ctx);
+        if (e != cudaSuccess) return e;
+    }
+    ctx->slot_kind[ctx->nslot] = kind;
+    return cudaEventRecord(ctx->ev[2 * ctx->nslot], ctx->st);
+}
+
+static cudaError_t prof_end(mhd_ctx *ctx)
+{
+    ctx->launches++;
+    if (!ctx->prof) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(ctx->ev[2 * ctx->nslot + 1], ctx->st);
+    ctx->nslot++;
+    return e;
+}
+
+/* launch one kernel (the call returns its launch status) with optional timing */
+#define LAUNCH(kind, call)            \
+    do {                              \
+        CK(prof_begin(ctx, kind));    \
+        CK(call);                     \
+        CK(prof_end(ctx));            \
+    } while (0)
 
 #define CK(call)                                   \
     do {                                           \
@@ -146,6 +203,10 @@ static void free_all(mhd_ctx *ctx)
     if (ctx->h_part) cudaFreeHost(ctx->h_part);
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    for (int q = 0; q < 2 * MAXSLOT; q++)
+        if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
+    for (int q = 0; q < 2; q++)
+        if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
     if (ctx->st) cudaStreamDestroy(ctx->st);
 }
 
@@ -339,7 +400,7 @@ static int put_state(mhd_ctx *ctx, void *dst, const double *src, long long n)
     for (long long off = 0; off < n; off += ctx->stage_n) {
         long long m = n - off < ctx->stage_n ? n - off : ctx->stage_n;
         CK(cudaMemcpyAsync(ctx->d_stage, src + off, m * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-        CK(launch_cvt(ctx->d_stage, (float *)dst + off, m, ctx->st));
+        LAUNCH(PK_CVT, launch_cvt(ctx->d_stage, (float *)dst + off, m, ctx->st));
     }
     return MHD_OK;
 }
@@ -352,7 +413,7 @@ static int get_state(mhd_ctx *ctx, double *dst, const void *src, long long n)
     }
     for (long long off = 0; off < n; off += ctx->stage_n) {
         long long m = n - off < ctx->stage_n ? n - off : ctx->stage_n;
-        CK(launch_cvt_back((const float *)src + off, ctx->d_stage, m, ctx->st));
+        LAUNCH(PK_CVT, launch_cvt_back((const float *)src + off, ctx->d_stage, m, ctx->st));
         CK(cudaMemcpyAsync(dst + off, ctx->d_stage, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
     }
@@ -382,6 +443,17 @@ extern "C" int mhd_upload(mhd_ctx *ctx, const double *U, const double *V, const 
     return MHD_OK;
 }
 
+extern "C" int mhd_upload_state(mhd_ctx *ctx, const double *U, const double *V)
+{
+    if (!ctx || !U || !V) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    int rc;
+    if ((rc = put_state(ctx, ctx->U, U, 9 * ctx->nc))) return rc;
+    ctx->vcur = 0;
+    if ((rc = put_state(ctx, ctx->Va, V, 9 * ctx->nc))) return rc;
+    return MHD_OK;
+}
+
 extern "C" int mhd_download(mhd_ctx *ctx, double *U, double *V)
 {
     if (!ctx) return MHD_ERR_ARG;
@@ -408,8 +480,8 @@ extern "C" int mhd_setdt(mhd_ctx *ctx, double *dt, double *ch, int ijk[3])
 {
     if (!ctx || !dt || !ch) return MHD_ERR_ARG;
     if (!ctx->uploaded) return MHD_ERR_STATE;
-    if (ctx->fp32) CK(launch_setdt(ctx->G, (const float *)vcur_ptr(ctx), ctx->d_part, ctx->npart, ctx->st));
-    else CK(launch_setdt(ctx->G, (const double *)vcur_ptr(ctx), ctx->d_part, ctx->npart, ctx->st));
+    if (ctx->fp32) LAUNCH(PK_SETDT, launch_setdt(ctx->G, (const float *)vcur_ptr(ctx), ctx->d_part, ctx->npart, ctx->st));
+    else LAUNCH(PK_SETDT, launch_setdt(ctx->G, (const double *)vcur_ptr(ctx), ctx->d_part, ctx->npart, ctx->st));
     CK(cudaMemcpyAsync(ctx->h_part, ctx->d_part, ctx->npart * sizeof(MaxLoc), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     MaxLoc best = {0.0, -1};
@@ -460,10 +532,12 @@ extern "C" int mhd_spiral_gravity(mhd_ctx *ctx, double t)
     } else {
         CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
         long long n = (long long)ixmax * jymax;
+        CK(prof_begin(ctx, PK_TRIG));
         trig_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->st>>>(ixmax, jymax, ctx->G.y, ctx->G.spL,
                                                                        (double)p->armnum, ctx->omdiff, ctx->d_sc,
                                                                        ctx->d_trig);
         CK(cudaGetLastError());
+        CK(prof_end(ctx));
     }
     return MHD_OK;
 }
@@ -486,16 +560,17 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     const T *V = (const T *)vcur_ptr(ctx);
     const T *Vinit = (const T *)ctx->Vinit;
     T *F = (T *)ctx->F, *Gf = (T *)ctx->Gf, *H = (T *)ctx->H;
-    CK(launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
-    CK(launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
-    CK(launch_flux(2, ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), false, ctx->st));
+    LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
+    LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
+    LAUNCH(PK_FLUX_Z, launch_flux(2, ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), false, ctx->st));
     StageArgs<T> a;
     a.V = V; a.F = F; a.G = Gf; a.H = H;
     a.Un = (T *)ctx->U; a.U1 = (T *)ctx->U1;
     a.Uinit = (const T *)ctx->Uinit; a.rhofloor = (const T *)ctx->rhofloor;
     a.Vout = (T *)vnext_ptr(ctx); a.Uraw = (T *)ctx->Uraw;
     a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.kind = kind; a.last = last; a.counters = counters;
-    CK(launch_update(ctx->G, a, ctx->st));
+    LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
+    LAUNCH(PK_GHOST, launch_ghost(ctx->G, a, ctx->st));
     ctx->vcur ^= 1;
     return MHD_OK;
 }
@@ -653,4 +728,64 @@ extern "C" int mhd_diagnostics(mhd_ctx *ctx, mhd_diag *d)
     (void)d;
     if (!ctx) return MHD_ERR_ARG;
     return MHD_ERR_ARG;
+}
+
+/* ------------------------------------------------------------------------ */
+/* instrumentation                                                           */
+/* ------------------------------------------------------------------------ */
+extern "C" int mhd_prof_enable(mhd_ctx *ctx, int on)
+{
+    if (!ctx) return MHD_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->st));
+    if (on && !ctx->ev[0])
+        for (int q = 0; q < 2 * MAXSLOT; q++) CK(cudaEventCreate(&ctx->ev[q]));
+    ctx->nslot = 0;
+    for (int k = 0; k < MHD_PROF_NKIND; k++) { ctx->prof_ms[k] = 0.0; ctx->prof_n[k] = 0; }
+    ctx->prof = on ? 1 : 0;
+    return MHD_OK;
+}
+
+extern "C" int mhd_prof_read(mhd_ctx *ctx, double *ms, long long *launches)
+{
+    if (!ctx) return MHD_ERR_ARG;
+    CK(prof_harvest(ctx));
+    for (int k = 0; k < MHD_PROF_NKIND; k++) {
+        if (ms) ms[k] = ctx->prof_ms[k];
+        if (launches) launches[k] = ctx->prof_n[k];
+    }
+    return MHD_OK;
+}
+
+extern "C" long long mhd_launch_count(const mhd_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int mhd_timer_start(mhd_ctx *ctx)
+{
+    if (!ctx) return MHD_ERR_ARG;
+    if (!ctx->tev[0]) {
+        CK(cudaEventCreate(&ctx->tev[0]));
+        CK(cudaEventCreate(&ctx->tev[1]));
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    CK(cudaEventRecord(ctx->tev[0], ctx->st));
+    return MHD_OK;
+}
+
+extern "C" int mhd_timer_stop(mhd_ctx *ctx, double *ms)
+{
+    if (!ctx || !ms || !ctx->tev[0]) return MHD_ERR_ARG;
+    CK(cudaEventRecord(ctx->tev[1], ctx->st));
+    CK(cudaEventSynchronize(ctx->tev[1]));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ctx->tev[0], ctx->tev[1]));
+    *ms = f;
+    return MHD_OK;
+}
+
+extern "C" int mhd_pin(void *ptr, size_t bytes, int on)
+{
+    mhd_ctx *ctx = NULL;
+    if (!ptr || !bytes) return MHD_ERR_ARG;
+    if (on) CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    else CK(cudaHostUnregister(ptr));
+    return MHD_OK;
 }

@@ -384,8 +384,12 @@ cudaError_t launch_update_t(const Geom &G, const StageArgs<T> &a, cudaStream_t s
     long long n = (long long)(G.ixmax - 2) * (G.jymax - 2) * (G.kzmax - 2);
     update_kernel<T><<<nblocks(n, 128), 128, 0, st>>>(G, a.V, a.F, a.G, a.H, a.Un, a.U1, a.Uinit, a.rhofloor,
                                                       a.Vout, a.Uraw, a.sc, a.trig, a.kind, a.last, a.counters);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_ghost_t(const Geom &G, const StageArgs<T> &a, cudaStream_t st)
+{
     long long ng = 2LL * G.ixmax * G.jymax + 2LL * G.ixmax * (G.kzmax - 2) + 2LL * (G.jymax - 2) * (G.kzmax - 2);
     T *Uo = (a.kind == 0 || a.kind == 1) ? a.U1 : a.Un;
     ghost_kernel<T><<<nblocks(ng, 128), 128, 0, st>>>(G, a.Uraw, Uo, a.Uinit, a.rhofloor, a.Vout, a.sc, a.last,
@@ -440,6 +444,10 @@ cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream
     cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st)                          \
     {                                                                                                        \
         return launch_update_t<T>(G, a, st);                                                                 \
+    }                                                                                                        \
+    cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st)                           \
+    {                                                                                                        \
+        return launch_ghost_t<T>(G, a, st);                                                                  \
     }                                                                                                        \
     cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st)            \
     {                                                                                                        \

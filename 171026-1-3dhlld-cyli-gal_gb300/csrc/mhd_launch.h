@@ -39,6 +39,7 @@ struct StageArgs {
     cudaError_t launch_states(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,     \
                               T *Vl, T *Vr, Box b, cudaStream_t st);                                         \
     cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                        \
+    cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                         \
     cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st);            \
     cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
                               double *S, cudaStream_t st);                                                   \

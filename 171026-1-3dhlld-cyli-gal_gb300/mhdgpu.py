@@ -110,6 +110,13 @@ def lib():
         "mhd_batch_download": (C.c_int, [vp, C.c_int, vp, vp]),
         "mhd_batch_step": (C.c_int, [vp, C.c_int, DP, IP]),
         "mhd_batch_tune": (C.c_int, [vp, IP]),
+        "mhd_upload_state": (C.c_int, [vp, vp, vp]),
+        "mhd_prof_enable": (C.c_int, [vp, C.c_int]),
+        "mhd_prof_read": (C.c_int, [vp, DP, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]),
+        "mhd_launch_count": (C.c_longlong, [vp]),
+        "mhd_timer_start": (C.c_int, [vp]),
+        "mhd_timer_stop": (C.c_int, [vp, _PD]),
+        "mhd_pin": (C.c_int, [vp, C.c_size_t, C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)
@@ -350,3 +357,36 @@ class Disc:
 
     def stream(self):
         return lib().mhd_stream(self.h)
+
+    def upload_state(self, U, V):
+        check(lib().mhd_upload_state(self.h, _ptr(U), _ptr(V)), "mhd_upload_state")
+
+    def download_into(self, U, V):
+        check(lib().mhd_download(self.h, _ptr(U), _ptr(V)), "mhd_download")
+
+    PROF_KINDS = ["flux_r", "flux_phi", "flux_z", "update", "ghost", "setdt", "trig", "convert"]
+
+    def prof(self, on=True):
+        check(lib().mhd_prof_enable(self.h, 1 if on else 0), "mhd_prof_enable")
+
+    def prof_read(self):
+        ms = np.zeros(8)
+        n = np.zeros(8, dtype=np.int64)
+        check(lib().mhd_prof_read(self.h, ms, n), "mhd_prof_read")
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PROF_KINDS)}
+
+    def launches(self):
+        return int(lib().mhd_launch_count(self.h))
+
+    def timer_start(self):
+        check(lib().mhd_timer_start(self.h), "mhd_timer_start")
+
+    def timer_stop(self):
+        ms = C.c_double()
+        check(lib().mhd_timer_stop(self.h, C.byref(ms)), "mhd_timer_stop")
+        return ms.value
+
+
+def pin(a, on=True):
+    """page-lock a numpy array's buffer for fast async copies"""
+    check(lib().mhd_pin(_ptr(a), a.nbytes, 1 if on else 0), "mhd_pin")

@@ -1,0 +1,332 @@
+#!/usr/bin/env python
+"""Benchmark: zone-updates/s of the cylindrical GLM-MHD TVD-RK3 step.
+
+Default workload (``disc5``): one 512x512x256 disc (67.1 M zones), beta = 1,
+cooling on, HLLD, minmod, RK3, CFL 0.4; seeded synthetic initial state (no
+dataset exists for this benchmark).  A "step" is one full RK3 step: CFL
+reduction, dt guard, three stages.
+
+* ``value``     the FP32 + FP64-repair form, state resident in HBM.
+* ``fp64``      the plain FP64 form (bit-identical to the reference C), same
+                workload, fewer steps.
+* ``e2e``       the FP32 form through the C-ABI with the reference host's own
+                FP64 arrays: every step uploads U, V from pinned host memory
+                (mhd_upload_state), steps, and downloads U, V (mhd_download).
+* ``roofline``  the kernel with the largest share of device time, timed live
+                with CUDA events around every launch on the context's stream.
+* ``cpu_baseline`` the oracle (C restatement of the reference algorithm) on
+                the host cores, on a bounded sample grid of the same physics.
+
+``--impl reference`` times that CPU implementation alone (the reference's
+own C cannot travel to the GPU machine; the restatement is bit-identical to it).
+The state is larger than L2 (129 MB), so timed steps run without a flush.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "zone-updates/s per RK3 step, FP32+FP64-repair vs plain FP64 on 1 GB300; HBM GB/s"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        if not sm:
+            return None
+        mx = max(float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit())
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_product():
+    import __graft_entry__ as ge
+    b = ge._load("mhd_build", os.path.join(ge.PKG, "build.py"))
+    b.build()
+    return ge._load("mhdgpu", os.path.join(ge.PKG, "mhdgpu.py"))
+
+
+def make_state(M, workload, dims):
+    (nr, nphi, nz), params, ic = M.workload(workload, nr=dims[0], nphi=dims[1], nz=dims[2])
+    grid = M.Grid.disc(nr, nphi, nz)
+    if params.gravity:
+        grid.set_initial_gravity()
+    U, V = grid.ic_disc(**ic)
+    return grid, params, U, V
+
+
+def with_precision(M, params, prec):
+    d = params.as_dict()
+    d.pop("precision")
+    return M.default_params(precision=prec, **d)
+
+
+def time_steps(M, disc, steps, warmup, prof=False, clocks=False):
+    t = 0.0
+    for _ in range(warmup):
+        rc, t, dt, ch, cnt = disc.step(t)
+        if rc != 0:
+            raise RuntimeError("dt guard fired in warm-up")
+    if prof:
+        disc.prof(True)
+    sampler = ClockSampler() if clocks else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.5)
+    n0 = disc.launches()
+    disc.timer_start()
+    w0 = time.perf_counter()
+    for _ in range(steps):
+        rc, t, dt, ch, cnt = disc.step(t)
+        if rc != 0:
+            raise RuntimeError("dt guard fired")
+    ms = disc.timer_stop()
+    wall = time.perf_counter() - w0
+    launches = disc.launches() - n0
+    ck = sampler.stop() if sampler else None
+    kern = disc.prof_read() if prof else None
+    if prof:
+        disc.prof(False)
+    return ms, wall, launches, kern, ck
+
+
+def cpu_baseline(M, workload, steps=None, min_seconds=10.0, dims=(128, 128, 64)):
+    """The oracle on all host cores on a bounded sample grid of the workload."""
+    import pyoracle
+    threads = os.cpu_count() or 1
+    grid, params, U, V = make_state(M, workload, dims)
+    o = pyoracle.Oracle(grid.spec.as_dict(), M.oracle_params(params), threads=threads)
+    if params.gravity:
+        o.initial_gravity()
+    o.load(U, V)
+    t = 0.0
+    rc, t, *_ = o.step(t)   # warm
+    n = 0
+    w0 = time.perf_counter()
+    while True:
+        rc, t, *_ = o.step(t)
+        n += 1
+        el = time.perf_counter() - w0
+        if steps is not None and n >= steps:
+            break
+        if steps is None and (el >= min_seconds or n >= 200):
+            break
+    o.close()
+    zones = dims[0] * dims[1] * dims[2]
+    return {"value": zones * n / el, "unit": "zone-updates/s", "cores": threads, "kind": "port",
+            "sample": "%d RK3 steps of the same physics on a %dx%dx%d grid (%d zones), oracle C "
+                      "restatement (bit-identical to the reference C) with OpenMP" %
+                      (n, dims[0], dims[1], dims[2], zones),
+            "seconds": el}
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def dist_init(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="disc5")
+    ap.add_argument("--size", default=None, help="NRxNPHIxNZ override")
+    ap.add_argument("--fp64-steps", type=int, default=None)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+    dims = tuple(int(v) for v in args.size.split("x")) if args.size else (512, 512, 256)
+    zones = dims[0] * dims[1] * dims[2]
+    cfg = {"workload": "%s: single disc %dx%dx%d (r in [0.1,1.5], phi in [0,2pi), z in [-0.5,0.5]), "
+                       "beta=1, cooling on, HLLD, minmod, TVD-RK3, CFL 0.4, seeded 1%% perturbation"
+                       % (args.workload, dims[0], dims[1], dims[2]),
+           "zones": zones, "l2": "state (>=2.5 GB) larger than L2; no flush needed"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        M = load_product()   # host helpers only (grid + initial state)
+        cb = cpu_baseline(M, args.workload, steps=max(args.steps, 1) + max(args.warmup, 0))
+        out = {"metric": METRIC, "value": cb["value"], "unit": "zone-updates/s", "n_gpus": args.gpus,
+               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+               "config": cfg,
+               "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+               "e2e": {"value": cb["value"], "unit": "zone-updates/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return 0
+
+    dist = dist_init(world)
+    import ctypes
+    M = load_product()
+    if world > 1:
+        # one independent replica per GPU (the batched discs do not exchange data)
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    grid, params, U, V = make_state(M, args.workload, dims)
+    hbm_peak, peak_kind = load_peaks()
+
+    # ---- FP32 + FP64-repair form, resident ----
+    p32 = with_precision(M, params, "fp32")
+    d32 = M.Disc(grid, p32)
+    d32.upload(U, V)
+    if dist:
+        dist.barrier()
+    ms, wall, launches, kern, clocks = time_steps(M, d32, args.steps, args.warmup, prof=True, clocks=(rank == 0))
+    if dist:
+        import torch
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = zones * args.steps * world / (ms / 1e3)
+
+    # dominant kernel and its roofline (algorithmic bytes, FP32 = 4 B per value)
+    tot = sum(v[0] for v in kern.values())
+    dom = max(kern, key=lambda k: kern[k][0])
+    dms, dn = kern[dom]
+    s = 4
+    nx, ny, nz_ = dims
+    per_launch = {
+        "flux_r": (nx + 1) * ny * nz_ * 18 * s,      # read V (9), write F (9) per face
+        "flux_phi": nx * (ny + 1) * nz_ * 18 * s,
+        "flux_z": nx * ny * (nz_ + 1) * 18 * s,
+        "update": zones * 64 * s,                    # V, F, G, H (27), U^n, U^k, rhofloor, U, V out
+        "ghost": 0, "setdt": zones * 8 * s, "trig": 0, "convert": 0,
+    }
+    achieved = per_launch[dom] / (dms / dn / 1e3) / 1e9 if dn else None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+            "algorithmic_bytes_per_launch": per_launch[dom], "avg_launch_ms": dms / dn if dn else None,
+            "note": "stencil with no contraction: the FP32/FP64 pipes, not HBM, bound these kernels; "
+                    "see profiles/ for pipe utilisation"}
+    shares = {k: round(v[0] / tot, 4) for k, v in kern.items() if v[1]}
+
+    # ---- e2e through the C-ABI with host FP64 buffers ----
+    e2e = None
+    if not args.no_e2e:
+        Uh = np.ascontiguousarray(U.copy())
+        Vh = np.ascontiguousarray(V.copy())
+        M.pin(Uh)
+        M.pin(Vh)
+        d32.timer_start()
+        t = 0.0
+        for _ in range(args.steps):
+            d32.upload_state(Uh, Vh)
+            rc, t, dt, ch, cnt = d32.step(t)
+            d32.download_into(Uh, Vh)
+        ems = d32.timer_stop()
+        M.pin(Uh, False)
+        M.pin(Vh, False)
+        nb = 2 * 9 * grid.ixmax * grid.jymax * grid.kzmax * 8
+        e2e = {"value": zones * args.steps * world / (ems / 1e3), "unit": "zone-updates/s",
+               "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "ms_per_step": ems / args.steps,
+               "what": "mhd_upload_state(U,V) + mhd_step + mhd_download(U,V), FP64 pinned host arrays"}
+        del Uh, Vh
+    d32.close()
+
+    # ---- plain FP64 form ----
+    f64_steps = args.fp64_steps or max(2, min(args.steps, 5))
+    p64 = with_precision(M, params, "fp64")
+    d64 = M.Disc(grid, p64)
+    d64.upload(U, V)
+    ms64, wall64, l64, kern64, _ = time_steps(M, d64, f64_steps, 1, prof=True)
+    d64.close()
+    v64 = zones * f64_steps * world / (ms64 / 1e3)
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(M, args.workload)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "zone-updates/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded disc initial state; no public dataset exists)",
+               "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
+               "gpu_launches": launches,
+               "kernel_share": shares,
+               "fp64": {"value": v64, "unit": "zone-updates/s", "steps": f64_steps,
+                        "ms_per_step": ms64 / f64_steps, "speedup_fp32_over_fp64": value / v64,
+                        "kernel_ms": {k: round(v[0] / max(v[1], 1), 3) for k, v in kern64.items() if v[1]}},
+               "hbm_gbs_algorithmic": zones * 300 / (ms / args.steps / 1e3) / 1e9}
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -167,6 +167,27 @@ int mhd_run(mhd_ctx *ctx, int nsteps, double *t);
 int mhd_diagnostics(mhd_ctx *ctx, mhd_diag *d);
 /* The CUDA stream the context launches on (as a cudaStream_t). */
 void *mhd_stream(mhd_ctx *ctx);
+/* Upload only the evolving state U, V (same layout as mhd_upload); the
+ * initial arrays and floors from the last mhd_upload stay. */
+int mhd_upload_state(mhd_ctx *ctx, const double *U, const double *V);
+
+/* ---- instrumentation ------------------------------------------------------ */
+/* Per-kernel timing with CUDA events recorded around every launch on the
+ * context's stream (off by default; enabling resets the totals).  Kinds:
+ * 0 flux r, 1 flux phi, 2 flux z, 3 update, 4 ghost fill, 5 CFL reduction,
+ * 6 arm-phase table, 7 state conversion. */
+#define MHD_PROF_NKIND 8
+int mhd_prof_enable(mhd_ctx *ctx, int on);
+int mhd_prof_read(mhd_ctx *ctx, double ms[MHD_PROF_NKIND], long long launches[MHD_PROF_NKIND]);
+/* Kernels this context has launched since creation. */
+long long mhd_launch_count(const mhd_ctx *ctx);
+/* Stream timer: start synchronises the stream and records an event; stop
+ * records a second event, waits for it and returns the elapsed device time. */
+int mhd_timer_start(mhd_ctx *ctx);
+int mhd_timer_stop(mhd_ctx *ctx, double *ms);
+/* Page-lock (on=1) or release (on=0) a caller's host buffer so the
+ * context's copies from/to it run asynchronously at full link speed. */
+int mhd_pin(void *ptr, size_t bytes, int on);
 
 /* ---- per-kernel probes (parity tests) ------------------------------------ */
 /* Reconstructed face states of one direction (dir 0 r, 1 phi, 2 z) with the
