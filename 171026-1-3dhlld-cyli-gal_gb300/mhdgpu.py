@@ -15,6 +15,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(PKG, "lib", "libmhdgpu.so")
 
 MHD_OK = 0
+MHD_ERR_ARG = -1
 MHD_ERR_DT = -3
 LIMITER = {"minmod": 0, "mc": 1}
 SOLVER = {"hlld": 0, "hll": 1}
