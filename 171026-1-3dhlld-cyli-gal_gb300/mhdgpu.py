@@ -118,6 +118,8 @@ def lib():
         "mhd_timer_start": (C.c_int, [vp]),
         "mhd_timer_stop": (C.c_int, [vp, _PD]),
         "mhd_pin": (C.c_int, [vp, C.c_size_t, C.c_int]),
+        "mhd_setdt_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        C.c_int, vp, _PD, _PD, IP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)

@@ -217,6 +217,24 @@ int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status);
  * the state is restored afterwards.  best[4] = {tile_i, tile_j, tile_k, threads}. */
 int mhd_batch_tune(mhd_batch *b, int *best);
 
+/* ---- allocation-free CFL reduction -------------------------------------- */
+/* No counterpart in the reference.  For callers that may not call cudaMalloc
+ * when they need a step size (a host that hands out device memory from its own
+ * pool and forbids allocation afterwards, a real-time loop): the same CFL
+ * reduction as mhd_setdt(), with its scratch in a fixed device array of
+ * MHD_NOALLOC_MAX_BLOCKS partials (about 128 KB, held by every GPU that loads
+ * the library until exit) instead of a context buffer; it allocates nothing.
+ * Inputs are device pointers: V [9][ix+2][jy+2][kz+2] FP64 and minlength
+ * [ix+2][kz+2]; dt, ch, ijk are host outputs as for mhd_setdt().  Grids whose
+ * CFL range (ix-10)*jy*kz exceeds MHD_NOALLOC_MAX_BLOCKS*256*64 cells
+ * (134,217,728) are rejected with MHD_ERR_ARG before any launch.  The first
+ * call on a device looks up the array's device address (make it before any
+ * stream capture).  Calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+#define MHD_NOALLOC_MAX_BLOCKS 8192
+int mhd_setdt_noalloc(const double *V, const double *minlength, int ix, int jy, int kz, double cfl,
+                      double minminlength, int cooling, void *stream, double *dt, double *ch, int ijk[3]);
+
 #ifdef __cplusplus
 }
 #endif
