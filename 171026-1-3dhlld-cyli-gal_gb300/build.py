@@ -5,7 +5,8 @@ Flags that matter for results:
 * plain FP64 kernels and the context code: ``--fmad=false`` with IEEE
   division and square root, so every expression rounds exactly as the
   reference C (built without contraction) does;
-* precision-form kernels: FP32 with multiply-add contraction allowed;
+* precision-form kernels: FP32 with multiply-add contraction and the fast
+  (2-ulp) FP32 division and square root;
 * host C: ``-ffp-contract=off`` (gcc contracts by default on Arm).
 """
 import concurrent.futures as cf
@@ -25,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-I", INCLUDE, "-I", CSRC,
                       "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]
 EXACT = ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
-FP32 = ["--fmad=true", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
+FP32 = ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 
 UNITS = {
     "mhd_ctx.cu": EXACT,

@@ -308,8 +308,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     size_t o_spR = put(spR.data(), kzmax), o_C1 = put(spC1.data(), ixmax), o_C2 = put(spC2.data(), ixmax);
     size_t o_D = put(spD.data(), ixmax), o_L = put(spL.data(), ixmax), o_y = put(g->y, jymax);
     size_t o_z = put(g->z, kzmax);
-    size_t nfl = (size_t)(o_cabs + (size_t)(g->irin + 1) * kzmax);   /* float copies: up to cabs */
-    std::vector<float> TF(T.begin(), T.begin() + nfl);
+    std::vector<float> TF(T.begin(), T.end());   /* FP32 copies at the same offsets */
 
 #define CKC(call)                                  \
     do {                                           \
@@ -335,6 +334,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     G.f.x = Fd + o_x; G.f.xm = Fd + o_xm; G.f.oneox = Fd + o_ox; G.f.oneodx = Fd + o_odx; G.f.oneodz = Fd + o_odz;
     G.f.g = Fd + o_g; G.f.xabs = Fd + o_xabs; G.f.zabs = Fd + o_zabs; G.f.cabs = Fd + o_cabs;
     G.f.oneody = (float)g->oneody;
+    G.d.minlength = D + o_minl; G.f.minlength = Fd + o_minl;
     G.minlength = D + o_minl; G.minminlength = g->minminlength; G.graxi = D + o_grax;
     G.spA = D + o_spA; G.spS = D + o_spS; G.spQ = D + o_spQ; G.spR = D + o_spR;
     G.spC1 = D + o_C1; G.spC2 = D + o_C2; G.spD = D + o_D; G.spL = D + o_L; G.y = D + o_y; G.z = D + o_z;
@@ -599,6 +599,7 @@ extern "C" int mhd_tvdrk(mhd_ctx *ctx, double dt, double ch, int counters[3])
     /* tvdrungekutta.h:33-34 (RK3 factor 1/3, live RK2 factor 1/2) */
     h->psicoef = ctx->p.scheme == MHD_SCHEME_RK2 ? exp(-dt * ch * MHD_ONEOCR * 0.5)
                                                  : exp(-dt * ch * MHD_ONEOCR * MHD_ONEO3);
+    h->dtf = (float)h->dt; h->chf = (float)h->ch; h->psif = (float)h->psicoef;
     h->dtbad = 0;
     CK(cudaMemcpyAsync(ctx->d_sc, h, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemsetAsync(ctx->d_cnt, 0, 9 * sizeof(int), ctx->st));
@@ -641,6 +642,7 @@ extern "C" int mhd_dbg_limiter(mhd_ctx *ctx, int dir, double dt, double *Vl, dou
     if (!ctx->uploaded) return MHD_ERR_STATE;
     ctx->h_sc->dt = dt;
     ctx->h_sc->psicoef = 1.0;
+    ctx->h_sc->dtf = (float)dt; ctx->h_sc->psif = 1.0f;
     CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
     long long nf = 9LL * (ctx->ixmax - 1) * (ctx->jymax - 1) * (ctx->kzmax - 1);
     CK(cudaMemsetAsync(ctx->F, 0, nf * ctx->esz, ctx->st));
@@ -665,6 +667,7 @@ extern "C" int mhd_dbg_flux(mhd_ctx *ctx, int dir, double dt, double ch, double 
     ctx->h_sc->dt = dt;
     ctx->h_sc->ch = ch;
     ctx->h_sc->psicoef = 1.0;
+    ctx->h_sc->dtf = (float)dt; ctx->h_sc->chf = (float)ch; ctx->h_sc->psif = 1.0f;
     CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
     long long nf = 9LL * (ctx->ixmax - 1) * (ctx->jymax - 1) * (ctx->kzmax - 1);
     CK(cudaMemsetAsync(ctx->F, 0, nf * ctx->esz, ctx->st));

@@ -31,15 +31,11 @@ __global__ void __launch_bounds__(128)
 flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
             T *__restrict__ F, Box b)
 {
-    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int nk = b.k1 - b.k0, nj = b.j1 - b.j0;
-    long long total = (long long)(b.i1 - b.i0) * nj * nk;
-    if (tid >= total) return;
-    int k = b.k0 + (int)(tid % nk);
-    long long r = tid / nk;
-    int j = b.j0 + (int)(r % nj);
-    int i = b.i0 + (int)(r / nj);
-    T dt = (T)sc->dt, ch = (T)sc->ch, psicoef = (T)sc->psicoef;
+    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = b.j0 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = b.i0 + blockIdx.z;
+    if (k >= b.k1 || j >= b.j1) return;
+    T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
     T L[9], R[9], Fo[9];
     face_states<T, DIR>(G, V, Vinit, i, j, k, dt, psicoef, L, R);
     face_flux<T, DIR>(G, L, R, i, ch, Fo);
@@ -62,16 +58,12 @@ __global__ void __launch_bounds__(128)
 states_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
               T *__restrict__ Vl, T *__restrict__ Vr, Box b)
 {
-    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int nk = b.k1 - b.k0, nj = b.j1 - b.j0;
-    long long total = (long long)(b.i1 - b.i0) * nj * nk;
-    if (tid >= total) return;
-    int k = b.k0 + (int)(tid % nk);
-    long long r = tid / nk;
-    int j = b.j0 + (int)(r % nj);
-    int i = b.i0 + (int)(r / nj);
+    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = b.j0 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = b.i0 + blockIdx.z;
+    if (k >= b.k1 || j >= b.j1) return;
     T L[9], R[9];
-    face_states<T, DIR>(G, V, Vinit, i, j, k, (T)sc->dt, (T)sc->psicoef, L, R);
+    face_states<T, DIR>(G, V, Vinit, i, j, k, Scal<T>::dt(sc), Scal<T>::psi(sc), L, R);
     long long nf = (long long)(G.ixmax - 1) * (G.jymax - 1) * (G.kzmax - 1);
     long long q = ((long long)i * (G.jymax - 1) + j) * (G.kzmax - 1) + k;
 #pragma unroll
@@ -124,22 +116,18 @@ update_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ F, const T 
               int *counters)
 {
     if (sc->dtbad) return;
-    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int nk = G.kzmax - 2, nj = G.jymax - 2;
-    long long total = (long long)(G.ixmax - 2) * nj * nk;
+    const int k = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = 1 + blockIdx.z;
     int flags = 0;
-    if (tid < total) {
-        int k = 1 + (int)(tid % nk);
-        long long r = tid / nk;
-        int j = 1 + (int)(r % nj);
-        int i = 1 + (int)(r / nj);
+    if (k < G.kzmax - 1 && j < G.jymax - 1) {
         const Tabs<T> &tb = tabs<T>(G);
         const long long nc = G.nc, q = cidx(G, i, j, k);
         const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
         const long long gk = (long long)i * G.kzmax + k, pl = (long long)G.ixmax * G.kzmax;
         const T g1 = tb.g[gk], g2 = tb.g[pl + gk], g3 = tb.g[2 * pl + gk];
         const T g4 = tb.g[3 * pl + gk], g5 = tb.g[4 * pl + gk], g6 = tb.g[5 * pl + gk];
-        const T dt = (T)sc->dt, psicoef = (T)sc->psicoef;
+        const T dt = Scal<T>::dt(sc), psicoef = Scal<T>::psi(sc);
         T W[9], S[9], u[9];
 #pragma unroll
         for (int m = 0; m < 9; m++) W[m] = V[m * nc + q];
@@ -208,25 +196,25 @@ ghost_kernel(Geom G, const T *__restrict__ Uraw, T *Uo, const T *__restrict__ Ui
              int last, int *counters)
 {
     if (sc->dtbad) return;
-    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
-    const long long nkplane = 2 * ni * nj;
-    const long long njplane = 2 * ni * (nk - 2);
-    const long long niplane = 2 * (nj - 2) * (nk - 2);
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
+    const unsigned nkplane = 2 * ni * nj;
+    const unsigned njplane = 2 * ni * (nk - 2);
+    const unsigned niplane = 2 * (nj - 2) * (nk - 2);
     int flags = 0;
     if (tid < nkplane + njplane + niplane) {
         int i, j, k;
         if (tid < nkplane) {
             k = (tid < ni * nj) ? 0 : (int)nk - 1;
-            long long r = tid % (ni * nj);
+            unsigned r = tid % (ni * nj);
             i = (int)(r / nj); j = (int)(r % nj);
         } else if (tid < nkplane + njplane) {
-            long long r = tid - nkplane;
+            unsigned r = tid - nkplane;
             j = (r < ni * (nk - 2)) ? 0 : (int)nj - 1;
             r %= ni * (nk - 2);
             i = (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
         } else {
-            long long r = tid - nkplane - njplane;
+            unsigned r = tid - nkplane - njplane;
             i = (r < (nj - 2) * (nk - 2)) ? 0 : (int)ni - 1;
             r %= (nj - 2) * (nk - 2);
             j = 1 + (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
@@ -263,33 +251,52 @@ __device__ __forceinline__ MaxLoc better(MaxLoc a, MaxLoc b)
     return a;
 }
 
+/* the CFL rate of one cell in FP64 (setdt.h:42-56) */
+template <typename T>
+__device__ __forceinline__ double cfl_rate64(const Geom &G, const T *__restrict__ V, int i, long long q, int k)
+{
+    const long long nc = G.nc;
+    double v0 = V[q], v1 = V[nc + q], v2v = V[2 * nc + q], v3 = V[3 * nc + q];
+    double v4 = V[4 * nc + q], v5 = V[5 * nc + q], v6 = V[6 * nc + q], v7 = V[7 * nc + q];
+    double v2 = v1 * v1 + v2v * v2v + v3 * v3;
+    double b2 = v4 * v4 + v5 * v5 + v6 * v6;
+    double t1 = sqrt(v2 + (MHD_GM * v7 + b2) / v0) / G.minlength[(long long)i * G.kzmax + k];
+    int cl = G.cooling ? cooling_rate(v0, v7) : 0;
+    double tc = (2.0 * ((v0 * v0 * cl) / (1.5 * v7)));
+    return rmax<double>(t1, tc);
+}
+
+/* Plain form: every cell in FP64, bit-identical to setdt.h.  Precision form:
+ * cells are screened in FP32 and each block's winner is re-evaluated in FP64,
+ * so the maximum (and dt) carries FP64 rounding of an FP32-selected cell. */
 template <typename T>
 __global__ void __launch_bounds__(256)
 setdt_kernel(Geom G, const T *__restrict__ V, MaxLoc *part)
 {
     __shared__ MaxLoc sm[8];
-    const int ilo = 1, ihi = G.ixmax - 1 - 10;
-    const long long nk = G.kzmax - 2, nj = G.jymax - 2;
-    const long long total = (long long)(ihi - ilo) * nj * nk;
+    const int nj = G.jymax - 2;
+    const int rows = (G.ixmax - 12) * nj;   /* i in [1, ixmax-11) (setdt.h:33) */
     MaxLoc best = {0.0, -1};
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        int k = 1 + (int)(t % nk);
-        long long r = t / nk;
-        int j = 1 + (int)(r % nj);
-        int i = ilo + (int)(r / nj);
-        const long long nc = G.nc, q = cidx(G, i, j, k);
-        double v0 = V[q], v1 = V[nc + q], v2v = V[2 * nc + q], v3 = V[3 * nc + q];
-        double v4 = V[4 * nc + q], v5 = V[5 * nc + q], v6 = V[6 * nc + q], v7 = V[7 * nc + q];
-        double v2 = v1 * v1 + v2v * v2v + v3 * v3;
-        double b2 = v4 * v4 + v5 * v5 + v6 * v6;
-        double t1 = sqrt(v2 + (MHD_GM * v7 + b2) / v0) / G.minlength[(long long)i * G.kzmax + k];
-        int cl = G.cooling ? cooling_rate(v0, v7) : 0;
-        double tc = (2.0 * ((v0 * v0 * cl) / (1.5 * v7)));
-        double tmp = rmax<double>(t1, tc);
-        /* the reference only takes a cell when tmp > running max (from 0) */
-        if (tmp > best.v || (best.q >= 0 && tmp == best.v && q < best.q)) {
-            if (tmp > 0.0) { best.v = tmp; best.q = q; }
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int i = 1 + r / nj, j = 1 + r % nj;
+        for (int k = 1 + threadIdx.x; k < G.kzmax - 1; k += blockDim.x) {
+            const long long q = cidx(G, i, j, k);
+            double tmp;
+            if (sizeof(T) == 8) {
+                tmp = cfl_rate64<T>(G, V, i, q, k);
+            } else {
+                const long long nc = G.nc;
+                float v0 = V[q], v1 = V[nc + q], v2v = V[2 * nc + q], v3 = V[3 * nc + q];
+                float v4 = V[4 * nc + q], v5 = V[5 * nc + q], v6 = V[6 * nc + q], v7 = V[7 * nc + q];
+                float v2 = v1 * v1 + v2v * v2v + v3 * v3;
+                float b2 = v4 * v4 + v5 * v5 + v6 * v6;
+                float t1 = sqrtf(v2 + ((float)MHD_GM * v7 + b2) / v0) / (float)G.f.minlength[(long long)i * G.kzmax + k];
+                int cl = G.cooling ? cooling_rate_f(v0, v7) : 0;
+                float tc = (2.0f * ((v0 * v0 * (float)cl) / (1.5f * v7)));
+                tmp = (double)rmax<float>(t1, tc);
+            }
+            /* the reference only takes a cell when its rate exceeds the running max (from 0) */
+            if (tmp > best.v && tmp > 0.0) { best.v = tmp; best.q = q; }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -303,6 +310,10 @@ setdt_kernel(Geom G, const T *__restrict__ V, MaxLoc *part)
     if (threadIdx.x == 0) {
         MaxLoc b = sm[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = better(b, sm[w]);
+        if (sizeof(T) == 4 && b.q >= 0) {
+            const int k = (int)(b.q % G.kzmax), i = (int)(b.q / ((long long)G.kzmax * G.jymax));
+            b.v = cfl_rate64<T>(G, V, i, b.q, k);
+        }
         part[blockIdx.x] = b;
     }
 }
@@ -348,14 +359,25 @@ __global__ void source_kernel(Geom G, const T *__restrict__ V, const StepScalars
 /* ------------------------------------------------------------------------ */
 static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+/* 128-thread blocks laid along k (fastest index), rows of j stacked when the
+ * k extent is short; one grid z-slice per i */
+static inline void grid3(int nk, int nj, int ni, dim3 &grid, dim3 &block)
+{
+    int bx = 32 * ((nk + 31) / 32);
+    if (bx > 128) bx = 128;
+    int by = 128 / bx;
+    block = dim3(bx, by, 1);
+    grid = dim3((nk + bx - 1) / bx, (nj + by - 1) / by, ni);
+}
+
 template <typename T>
 cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,
                           Box b, bool reflayout, cudaStream_t st)
 {
-    long long n = (long long)(b.i1 - b.i0) * (b.j1 - b.j0) * (b.k1 - b.k0);
-    if (n <= 0) return cudaSuccess;
-    unsigned nb = nblocks(n, 128);
-#define MHD_FLUX_CASE(D, RL) flux_kernel<T, D, RL><<<nb, 128, 0, st>>>(G, V, Vinit, sc, F, b)
+    if (b.i1 <= b.i0 || b.j1 <= b.j0 || b.k1 <= b.k0) return cudaSuccess;
+    dim3 gr, bl;
+    grid3(b.k1 - b.k0, b.j1 - b.j0, b.i1 - b.i0, gr, bl);
+#define MHD_FLUX_CASE(D, RL) flux_kernel<T, D, RL><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b)
     if (reflayout) {
         if (dir == 0) MHD_FLUX_CASE(0, true); else if (dir == 1) MHD_FLUX_CASE(1, true); else MHD_FLUX_CASE(2, true);
     } else {
@@ -369,20 +391,21 @@ template <typename T>
 cudaError_t launch_states_t(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *Vl,
                             T *Vr, Box b, cudaStream_t st)
 {
-    long long n = (long long)(b.i1 - b.i0) * (b.j1 - b.j0) * (b.k1 - b.k0);
-    if (n <= 0) return cudaSuccess;
-    unsigned nb = nblocks(n, 128);
-    if (dir == 0) states_kernel<T, 0><<<nb, 128, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
-    else if (dir == 1) states_kernel<T, 1><<<nb, 128, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
-    else states_kernel<T, 2><<<nb, 128, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
+    if (b.i1 <= b.i0 || b.j1 <= b.j0 || b.k1 <= b.k0) return cudaSuccess;
+    dim3 gr, bl;
+    grid3(b.k1 - b.k0, b.j1 - b.j0, b.i1 - b.i0, gr, bl);
+    if (dir == 0) states_kernel<T, 0><<<gr, bl, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
+    else if (dir == 1) states_kernel<T, 1><<<gr, bl, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
+    else states_kernel<T, 2><<<gr, bl, 0, st>>>(G, V, Vinit, sc, Vl, Vr, b);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_update_t(const Geom &G, const StageArgs<T> &a, cudaStream_t st)
 {
-    long long n = (long long)(G.ixmax - 2) * (G.jymax - 2) * (G.kzmax - 2);
-    update_kernel<T><<<nblocks(n, 128), 128, 0, st>>>(G, a.V, a.F, a.G, a.H, a.Un, a.U1, a.Uinit, a.rhofloor,
+    dim3 gr, bl;
+    grid3(G.kzmax - 2, G.jymax - 2, G.ixmax - 2, gr, bl);
+    update_kernel<T><<<gr, bl, 0, st>>>(G, a.V, a.F, a.G, a.H, a.Un, a.U1, a.Uinit, a.rhofloor,
                                                       a.Vout, a.Uraw, a.sc, a.trig, a.kind, a.last, a.counters);
     return cudaGetLastError();
 }
