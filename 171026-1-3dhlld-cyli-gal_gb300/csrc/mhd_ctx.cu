@@ -52,7 +52,8 @@ struct mhd_ctx {
     cudaError_t last_cuda;
     /* mhd_run graph */
     cudaGraphExec_t gexec;
-    int graph_ready;
+    cudaGraphExec_t gexecs[2];
+    int graph_ready, graph_launches;
     int *d_cnt_run;
     /* instrumentation */
     long long launches;
@@ -203,6 +204,8 @@ static void free_all(mhd_ctx *ctx)
     if (ctx->h_part) cudaFreeHost(ctx->h_part);
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    for (int q = 0; q < 2; q++)
+        if (ctx->gexecs[q]) cudaGraphExecDestroy(ctx->gexecs[q]);
     for (int q = 0; q < 2 * MAXSLOT; q++)
         if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
     for (int q = 0; q < 2; q++)
@@ -289,6 +292,10 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
         spQ[k] = (1.0 + a1 / sqrt(z2 + b1 * b1));
         spR[k] = 1.0 / (z2 + p->scalez * p->scalez);
     }
+    std::vector<double> dvol(nik, 0.0);
+    for (int i = 1; i < ixmax - 1; i++)
+        for (int k = 1; k < kzmax - 1; k++)
+            dvol[(size_t)i * kzmax + k] = 0.5 * (g->xm[i] * g->xm[i] - g->xm[i - 1] * g->xm[i - 1]) * g->dy * g->dzm[k - 1];
     ctx->hx.assign(g->x, g->x + ixmax);
     ctx->hy.assign(g->y, g->y + jymax);
     ctx->hspL = spL;
@@ -308,6 +315,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     size_t o_spR = put(spR.data(), kzmax), o_C1 = put(spC1.data(), ixmax), o_C2 = put(spC2.data(), ixmax);
     size_t o_D = put(spD.data(), ixmax), o_L = put(spL.data(), ixmax), o_y = put(g->y, jymax);
     size_t o_z = put(g->z, kzmax);
+    size_t o_dvol = put(dvol.data(), nik);
     std::vector<float> TF(T.begin(), T.end());   /* FP32 copies at the same offsets */
 
 #define CKC(call)                                  \
@@ -338,6 +346,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     G.minlength = D + o_minl; G.minminlength = g->minminlength; G.graxi = D + o_grax;
     G.spA = D + o_spA; G.spS = D + o_spS; G.spQ = D + o_spQ; G.spR = D + o_spR;
     G.spC1 = D + o_C1; G.spC2 = D + o_C2; G.spD = D + o_D; G.spL = D + o_L; G.y = D + o_y; G.z = D + o_z;
+    G.dvol = D + o_dvol; G.dy = g->dy;
     G.omegasp = p->omegasp; G.prcr = p->prcr; G.betacr = p->betacr; G.rhocr = p->rhocr;
     G.armnum = (double)p->armnum; G.cotpitch = cotpitch;
     G.cooling = p->cooling; G.gravity = p->gravity; G.limiter = p->limiter; G.solver = p->solver;
@@ -719,18 +728,201 @@ extern "C" int mhd_dbg_gravity(mhd_ctx *ctx, double *gr)
     return MHD_OK;
 }
 
+/* ------------------------------------------------------------------------ */
+/* device-resident stepping (precision form)                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Fold the CFL partials and set this step's scalars on the device:
+ * setdt.h:84,89, the guard of main.c:331, the psi factor of
+ * tvdrungekutta.h:33-34 and the spiral amplitude of spiralgravity.h:41-42. */
+__global__ void step_scalars_kernel(const MaxLoc *__restrict__ part, int n, double cfl, double minminlength,
+                                    double dtmin, double psifac, double tausp, double epssp0, StepScalars *sc)
+{
+    __shared__ MaxLoc sm[32];
+    MaxLoc best = {0.0, -1};
+    for (int b = threadIdx.x; b < n; b += blockDim.x) {
+        MaxLoc o = part[b];
+        if (o.q >= 0 && (best.q < 0 || o.v > best.v || (o.v == best.v && o.q < best.q))) best = o;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        MaxLoc x;
+        x.v = __shfl_down_sync(0xffffffffu, best.v, o);
+        x.q = __shfl_down_sync(0xffffffffu, best.q, o);
+        if (x.q >= 0 && (best.q < 0 || x.v > best.v || (x.v == best.v && x.q < best.q))) best = x;
+    }
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+        MaxLoc x = sm[w];
+        if (x.q >= 0 && (best.q < 0 || x.v > best.v || (x.v == best.v && x.q < best.q))) best = x;
+    }
+    if (sc->dtbad) return;   /* a fired guard freezes the state and t */
+    double oneocfldt = best.q >= 0 ? best.v : 0.0;
+    double dt = cfl / oneocfldt, ch = minminlength * oneocfldt;
+    sc->oneocfldt = oneocfldt;
+    sc->argmax = best.q;
+    if (isinf(dt) || dt < dtmin) { sc->dtbad = 1; return; }
+    double t = sc->t;
+    double sw = (t - tausp) / fabs(t - tausp);
+    sc->epssp = 0.5 * epssp0 * (t / tausp * (1.0 - sw) + (1.0 + sw));
+    sc->dt = dt;
+    sc->ch = ch;
+    sc->psicoef = exp(-dt * ch * MHD_ONEOCR * psifac);
+    sc->dtf = (float)dt;
+    sc->chf = (float)ch;
+    sc->psif = (float)sc->psicoef;
+}
+
+__global__ void advance_t_kernel(StepScalars *sc)
+{
+    if (!sc->dtbad) sc->t += sc->dt;
+}
+
+/* the launches of one whole step, device-resident */
+static int enqueue_device_step(mhd_ctx *ctx)
+{
+    const mhd_params *p = &ctx->p;
+    CK(launch_setdt(ctx->G, (const float *)vcur_ptr(ctx), ctx->d_part, ctx->npart, ctx->st));
+    ctx->launches++;
+    double psifac = p->scheme == MHD_SCHEME_RK2 ? 0.5 : MHD_ONEO3;
+    step_scalars_kernel<<<1, 1024, 0, ctx->st>>>(ctx->d_part, ctx->npart, p->cfl, ctx->G.minminlength, p->dtmin,
+                                                 psifac, p->tausp, p->epssp0, ctx->d_sc);
+    CK(cudaGetLastError());
+    ctx->launches++;
+    if (p->gravity) {
+        long long n = (long long)ctx->ixmax * ctx->jymax;
+        trig_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->st>>>(ctx->ixmax, ctx->jymax, ctx->G.y,
+                                                                       ctx->G.spL, (double)p->armnum,
+                                                                       ctx->omdiff, ctx->d_sc, ctx->d_trig);
+        CK(cudaGetLastError());
+        ctx->launches++;
+    }
+    int rc = run_stages(ctx, ctx->d_cnt_run);
+    if (rc) return rc;
+    advance_t_kernel<<<1, 1, 0, ctx->st>>>(ctx->d_sc);
+    CK(cudaGetLastError());
+    ctx->launches++;
+    return MHD_OK;
+}
+
 extern "C" int mhd_run(mhd_ctx *ctx, int nsteps, double *t)
 {
-    (void)nsteps; (void)t;
-    if (!ctx) return MHD_ERR_ARG;
-    return MHD_ERR_ARG;   /* device-resident stepping: not built yet */
+    if (!ctx || !t || nsteps < 0) return MHD_ERR_ARG;
+    if (!ctx->fp32) return MHD_ERR_ARG;   /* plain form: host exp/sincos for bitwise parity */
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    if (!ctx->d_cnt_run) CK(cudaMalloc((void **)&ctx->d_cnt_run, 9 * sizeof(int)));
+    StepScalars *h = ctx->h_sc;
+    h->t = *t;
+    h->dtbad = 0;
+    CK(cudaMemcpyAsync(ctx->d_sc, h, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
+    /* the graph bakes in which primitive buffer is current: capture one per
+     * starting parity (an odd stage count flips it every step) */
+    int nst = ctx->p.scheme == MHD_SCHEME_RK2 ? 2 : 3;
+    if (!ctx->graph_ready) {
+        int prof = ctx->prof;
+        ctx->prof = 0;
+        int v0 = ctx->vcur;
+        long long l0 = ctx->launches;
+        for (int vs = 0; vs < 2; vs++) {
+            cudaGraph_t graph;
+            ctx->vcur = vs;
+            CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_device_step(ctx);
+            cudaError_t e = cudaStreamEndCapture(ctx->st, &graph);
+            if (rc) { ctx->prof = prof; ctx->vcur = v0; return rc; }
+            CK(e);
+            CK(cudaGraphInstantiate(&ctx->gexecs[vs], graph, 0));
+            cudaGraphDestroy(graph);
+        }
+        ctx->graph_launches = (int)((ctx->launches - l0) / 2);
+        ctx->launches = l0;
+        ctx->vcur = v0;
+        ctx->prof = prof;
+        ctx->graph_ready = 1;
+    }
+    for (int s = 0; s < nsteps; s++) {
+        CK(cudaGraphLaunch(ctx->gexecs[ctx->vcur], ctx->st));
+        ctx->vcur ^= (nst & 1);
+        ctx->launches += ctx->graph_launches;
+    }
+    CK(cudaMemcpyAsync(h, ctx->d_sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    *t = h->t;
+    return h->dtbad ? MHD_ERR_DT : MHD_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* diagnostics                                                               */
+/* ------------------------------------------------------------------------ */
+template <typename T>
+__global__ void __launch_bounds__(256) diag_kernel(Geom G, const T *__restrict__ U, double *part)
+{
+    __shared__ double sm[5][8];
+    const int nj = G.jymax - 2, rows = (G.ixmax - 2) * nj;
+    const long long nc = G.nc;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0}, dmax = 0.0;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int i = 1 + r / nj, j = 1 + r % nj;
+        const double xi = G.d.x[i], xp = G.d.x[i + 1], xmn = G.d.x[i - 1];
+        for (int k = 1 + threadIdx.x; k < G.kzmax - 1; k += blockDim.x) {
+            const long long q = cidx(G, i, j, k);
+            const double dv = G.dvol[(long long)i * G.kzmax + k];
+            acc[0] += (double)U[q] * dv;
+            acc[1] += (double)U[2 * nc + q] * dv;
+            acc[2] += (double)U[7 * nc + q] * dv;
+            acc[3] += fabs((double)U[8 * nc + q]) * dv;
+            const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
+            double divb = (xp * (double)U[4 * nc + q + si] - xmn * (double)U[4 * nc + q - si]) / (xi * (xp - xmn))
+                          + ((double)U[5 * nc + q + sj] - (double)U[5 * nc + q - sj]) / (xi * 2.0 * G.dy)
+                          + ((double)U[6 * nc + q + 1] - (double)U[6 * nc + q - 1]) / (G.z[k + 1] - G.z[k - 1]);
+            dmax = fmax(dmax, fabs(divb));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int c = 0; c < 4; c++) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], o);
+        dmax = fmax(dmax, __shfl_down_sync(0xffffffffu, dmax, o));
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        for (int c = 0; c < 4; c++) sm[c][w] = acc[c];
+        sm[4][w] = dmax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double out[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int v = 0; v < (int)(blockDim.x >> 5); v++) {
+            for (int c = 0; c < 4; c++) out[c] += sm[c][v];
+            out[4] = fmax(out[4], sm[4][v]);
+        }
+        for (int c = 0; c < 5; c++) part[blockIdx.x * 5 + c] = out[c];
+    }
 }
 
 extern "C" int mhd_diagnostics(mhd_ctx *ctx, mhd_diag *d)
 {
-    (void)d;
-    if (!ctx) return MHD_ERR_ARG;
-    return MHD_ERR_ARG;
+    if (!ctx || !d) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    const int nblk = 1024;
+    double *dp = NULL;
+    std::vector<double> hp(5 * nblk);
+    CK(cudaMallocAsync((void **)&dp, 5 * nblk * sizeof(double), ctx->st));
+    if (ctx->fp32) diag_kernel<float><<<nblk, 256, 0, ctx->st>>>(ctx->G, (const float *)ctx->U, dp);
+    else diag_kernel<double><<<nblk, 256, 0, ctx->st>>>(ctx->G, (const double *)ctx->U, dp);
+    cudaError_t e = cudaGetLastError();
+    ctx->launches++;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hp.data(), dp, 5 * nblk * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+    cudaFreeAsync(dp, ctx->st);
+    CK(e);
+    CK(cudaStreamSynchronize(ctx->st));
+    double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < nblk; b++) {
+        for (int c = 0; c < 4; c++) s[c] += hp[5 * b + c];
+        s[4] = fmax(s[4], hp[5 * b + 4]);
+    }
+    d->mass = s[0]; d->angmom = s[1]; d->energy = s[2]; d->psi = s[3]; d->maxdivb = s[4];
+    return MHD_OK;
 }
 
 /* ------------------------------------------------------------------------ */

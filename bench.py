@@ -180,6 +180,59 @@ def cpu_baseline(M, workload, steps=None, min_seconds=10.0, dims=(128, 128, 64))
             "seconds": el}
 
 
+def precision_report(args):
+    """FP32 + FP64-repair form against the plain FP64 form (bit-identical to the
+    reference C, checked on smaller grids by the tests) after N steps from the
+    same state: per conserved variable relative L1 and Linf, and the drift of
+    the totals and max|div B| of both forms."""
+    M = load_product()
+    dims = tuple(int(v) for v in args.size.split("x")) if args.size else (256, 256, 128)
+    (nr, nphi, nz), params, ic = M.workload(args.workload, nr=dims[0], nphi=dims[1], nz=dims[2],
+                                             **({"solver": args.solver} if args.solver else {}))
+    grid = M.Grid.disc(nr, nphi, nz)
+    if params.gravity:
+        grid.set_initial_gravity()
+    U, V = grid.ic_disc(**ic)
+    out = {"report": "precision", "workload": args.workload, "dims": dims, "steps": args.precision_report,
+           "solver": "hll" if params.solver == 1 else "hlld"}
+    res = {}
+    for prec in ("fp64", "fp32"):
+        d = M.Disc(grid, with_precision(M, params, prec))
+        d.upload(U, V)
+        d0 = d.diagnostics()
+        t = 0.0
+        w0 = time.perf_counter()
+        maxdivb = d0["maxdivb"]
+        psi_max = 0.0
+        for n in range(args.precision_report):
+            rc, t, dt, ch, cnt = d.step(t)
+            if rc != 0:
+                raise RuntimeError("dt guard fired at step %d" % n)
+            if (n + 1) % 10 == 0 or n + 1 == args.precision_report:
+                dg = d.diagnostics()
+                maxdivb = max(maxdivb, dg["maxdivb"])
+                psi_max = max(psi_max, dg["psi"])
+        wall = time.perf_counter() - w0
+        d1 = d.diagnostics()
+        Uf, _ = d.download()
+        d.close()
+        res[prec] = Uf
+        out[prec] = {"t": t, "wall_s": wall,
+                     "drift": {k: (d1[k] - d0[k]) / abs(d0[k]) if d0[k] else d1[k] for k in ("mass", "angmom", "energy")},
+                     "maxdivb_end": d1["maxdivb"], "maxdivb_max": maxdivb, "psi_total_max": psi_max}
+    a, b = res["fp32"], res["fp64"]
+    names = ["rho", "m_r", "r*m_phi", "m_z", "B_r", "B_phi", "B_z", "E", "psi"]
+    rl1, linf = {}, {}
+    for m in range(9):
+        den = np.abs(b[m]).sum()
+        rl1[names[m]] = float(np.abs(a[m] - b[m]).sum() / den) if den > 0 else float(np.abs(a[m] - b[m]).sum())
+        sc = np.abs(b[m]).max()
+        linf[names[m]] = float(np.abs(a[m] - b[m]).max() / sc) if sc > 0 else float(np.abs(a[m] - b[m]).max())
+    out["fp32_vs_fp64"] = {"rel_l1": rl1, "rel_linf": linf}
+    print(json.dumps(out))
+    return 0
+
+
 def rank_info():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -204,7 +257,12 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precision-report", type=int, default=0, metavar="NSTEPS",
+                    help="run both forms NSTEPS steps and report the FP32 form's error")
+    ap.add_argument("--solver", default=None, help="hlld or hll")
     args = ap.parse_args()
+    if args.precision_report:
+        return precision_report(args)
     rank, world, local = rank_info()
     dims = tuple(int(v) for v in args.size.split("x")) if args.size else (512, 512, 256)
     zones = dims[0] * dims[1] * dims[2]

@@ -51,3 +51,26 @@ def rel_l1(a, b):
         num = np.abs(a[m] - b[m]).sum()
         out.append(num / den if den > 0 else num)
     return np.array(out)
+
+
+def diagnostics_np(grid, U):
+    """The library's mhd_diagnostics definition restated in numpy (FP64)."""
+    x = grid.arr("x", grid.ixmax)
+    xm = grid.arr("xm", grid.ixmax)
+    dzm = grid.arr("dzm", grid.kzmax)
+    z = grid.arr("z", grid.kzmax)
+    dy = grid.g.dy
+    dv = 0.5 * (xm[1:-1] ** 2 - xm[:-2] ** 2)[:, None] * dy * dzm[:-2][None, :]
+    dv = dv[:, None, :]
+    I = (slice(1, -1),) * 3
+    out = {"mass": float((U[0][I] * dv).sum()), "angmom": float((U[2][I] * dv).sum()),
+           "energy": float((U[7][I] * dv).sum()), "psi": float((np.abs(U[8][I]) * dv).sum())}
+    xi = x[1:-1][:, None, None]
+    xp = x[2:][:, None, None]
+    xn = x[:-2][:, None, None]
+    br, bp, bz = U[4], U[5], U[6]
+    divb = ((xp * br[2:, 1:-1, 1:-1] - xn * br[:-2, 1:-1, 1:-1]) / (xi * (xp - xn))
+            + (bp[1:-1, 2:, 1:-1] - bp[1:-1, :-2, 1:-1]) / (xi * 2.0 * dy)
+            + (bz[1:-1, 1:-1, 2:] - bz[1:-1, 1:-1, :-2]) / (z[2:] - z[:-2])[None, None, :])
+    out["maxdivb"] = float(np.abs(divb).max())
+    return out
