@@ -1,21 +1,507 @@
 /*
  * mhd_batch.cu -- many independent discs of uneven sizes and parameters.
  *
- * This first form keeps one context per disc and steps the discs in turn,
- * each with its own dt (the reference has no batched driver; each disc is a
- * run of main.c:316-393).  A disc whose dt guard fires (main.c:331) stops and
- * reports MHD_ERR_DT in its status slot; the others continue.
+ * The reference has no batched driver: each disc is one run of main.c:316-393
+ * with its own Setdt/SpiralGravity/TVDRK.  Here every disc keeps its own
+ * context (state, tables, dt), and a step of ALL discs is:
+ *
+ *   CFL reduction   one launch over row tiles of every disc (per-disc partials)
+ *   step scalars    one block per disc: its dt, ch, psi factor, spiral
+ *                   amplitude and dt guard (setdt.h:84-89, main.c:331,
+ *                   tvdrungekutta.h:33-34, spiralgravity.h:41-42)
+ *   arm phase       cos/sin per (i,j) of every disc with gravity
+ *   3 RK stages     ONE persistent launch per stage: blocks take tiles from a
+ *                   global queue ordered [flux tiles of all discs][update
+ *                   tiles][ghost tiles]; an update tile waits (bounded spin)
+ *                   until its disc's flux tiles are done, a ghost tile until
+ *                   its disc's update tiles are done.  Every tile a block waits
+ *                   for was taken earlier by a running block, so the waits end.
+ *   advance         t += dt per disc whose guard did not fire
+ *
+ * captured as one CUDA graph per primitive-buffer parity.  Tile shape (r x phi
+ * x z cells per tile), threads per block and the register cap (launch
+ * bounds) are chosen by mhd_batch_tune(), which times candidates on the live
+ * state and restores it.  The halo is read through L1 from global memory, so
+ * its depth is the stencil's (2 cells) for every tile shape.
+ *
+ * Precision form only (FP32 + FP64 repair, the per-cell code of the
+ * single-disc kernels); a batch of plain FP64 discs is stepped disc by disc
+ * through mhd_step, each bit-identical to the reference.
  */
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <string.h>
+
 #include <new>
 #include <vector>
 
-#include "mhd_gpu.h"
+#include "mhd_ctx_internal.h"
+#include "mhd_kernels.cuh"
+
+using namespace mhd;
+
+namespace {
+
+struct DiscDev {
+    Geom G;
+    float *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
+    StepScalars *sc;
+    double *trig;
+    MaxLoc *part;
+    int *counters;          /* [3 stages][3] */
+    Box fbox[3], ubox;      /* flux face boxes per direction, interior box */
+    int ft[3][3];           /* flux tiles along i, j, k per direction */
+    int ut[3];              /* update tiles along i, j, k */
+    int nflux, nupd, nghost, ndt;
+    double cfl, minminlength, dtmin, psifac, tausp, epssp0, omdiff, armnum;
+    int gravity;
+};
+
+struct TileCfg {
+    int ti, tj, tk, bt, variant;
+};
+
+/* candidate configurations: tile ti x tj x tk cells, bt threads, launch-bounds
+ * variant (register cap 65536/(bt*minblocks)) */
+static const TileCfg CANDIDATES[] = {
+    {1, 1, 128, 128, 0}, {1, 2, 64, 128, 0}, {1, 4, 32, 128, 0}, {2, 2, 32, 128, 0},
+    {1, 2, 64, 128, 1},  {1, 4, 64, 256, 2}, {1, 2, 128, 256, 3}, {1, 1, 64, 64, 4},
+};
+static const int NCAND = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
+#define MHD_SPIN_LIMIT (1 << 24)
+
+__device__ __forceinline__ void add_counts(int a, int b, int c, int *counters)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (a | b | c)) {
+        if (a) atomicAdd(&counters[0], a);
+        if (b) atomicAdd(&counters[1], b);
+        if (c) atomicAdd(&counters[2], c);
+    }
+}
+
+/* bounded wait until *flag >= target; false (and the error flag set) if the
+ * limit runs out */
+__device__ __forceinline__ bool wait_at_least(int *flag, int target, int *err)
+{
+    for (int it = 0; it < MHD_SPIN_LIMIT; it++) {
+        if (atomicAdd(flag, 0) >= target) {
+            __threadfence();
+            return true;
+        }
+        if (atomicAdd(err, 0)) return false;
+        __nanosleep(256);
+    }
+    atomicExch(err, 1);
+    return false;
+}
+
+template <int BT, int MINB>
+__global__ void __launch_bounds__(BT, MINB)
+batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ tiles, int ntiles, int *head,
+                   int *done, int ndisc, int *err, int kind, int last, int parity, int stage, TileCfg cfg)
+{
+    __shared__ int s_t, s_ok;
+    for (;;) {
+        if (threadIdx.x == 0) s_t = atomicAdd(head, 1);
+        __syncthreads();
+        const int t = s_t;
+        if (t >= ntiles) return;
+        const uint2 e = tiles[t];
+        const int d = (int)e.x, code = (int)(e.y >> 28), local = (int)(e.y & 0x0fffffffu);
+        const DiscDev &D = discs[d];
+        if (threadIdx.x == 0) {
+            int ok = 1;
+            if (code == 3) ok = wait_at_least(&done[d], D.nflux, err);
+            else if (code == 4) ok = wait_at_least(&done[ndisc + d], D.nupd, err);
+            s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        const bool live = !D.sc->dtbad;
+        const float *V = parity ? D.Vb : D.Va;
+        if (live && code < 3) {
+            const Box &b = D.fbox[code];
+            const int ntk = D.ft[code][2], ntj = D.ft[code][1];
+            const int tk = local % ntk, tj = (local / ntk) % ntj, tii = local / (ntk * ntj);
+            const int n = cfg.ti * cfg.tj * cfg.tk;
+            float *Fd = code == 0 ? D.F : code == 1 ? D.Gf : D.H;
+            for (int c = threadIdx.x; c < n; c += BT) {
+                const int kk = c % cfg.tk, jj = (c / cfg.tk) % cfg.tj, ii = c / (cfg.tk * cfg.tj);
+                const int i = b.i0 + tii * cfg.ti + ii, j = b.j0 + tj * cfg.tj + jj, k = b.k0 + tk * cfg.tk + kk;
+                if (i >= b.i1 || j >= b.j1 || k >= b.k1) continue;
+                if (code == 0) flux_face<float, 0, false>(D.G, V, D.Vinit, D.sc, Fd, i, j, k);
+                else if (code == 1) flux_face<float, 1, false>(D.G, V, D.Vinit, D.sc, Fd, i, j, k);
+                else flux_face<float, 2, false>(D.G, V, D.Vinit, D.sc, Fd, i, j, k);
+            }
+        } else if (live) {
+            StageArgs<float> a;
+            a.V = V; a.F = D.F; a.G = D.Gf; a.H = D.H; a.Un = D.U; a.U1 = D.U1;
+            a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw;
+            a.sc = D.sc; a.trig = D.trig; a.kind = kind; a.last = last; a.counters = D.counters + 3 * stage;
+            int c0 = 0, c1 = 0, c2 = 0;
+            if (code == 3) {
+                const Box &b = D.ubox;
+                const int ntk = D.ut[2], ntj = D.ut[1];
+                const int tk = local % ntk, tj = (local / ntk) % ntj, tii = local / (ntk * ntj);
+                const int n = cfg.ti * cfg.tj * cfg.tk;
+                for (int c = threadIdx.x; c < n; c += BT) {
+                    const int kk = c % cfg.tk, jj = (c / cfg.tk) % cfg.tj, ii = c / (cfg.tk * cfg.tj);
+                    const int i = b.i0 + tii * cfg.ti + ii, j = b.j0 + tj * cfg.tj + jj, k = b.k0 + tk * cfg.tk + kk;
+                    if (i >= b.i1 || j >= b.j1 || k >= b.k1) continue;
+                    int f = update_cell<float>(D.G, a, i, j, k);
+                    c0 += f & 1; c1 += (f >> 1) & 1; c2 += (f >> 2) & 1;
+                }
+            } else {
+                const unsigned ng = ghost_count(D.G);
+                const unsigned g0 = (unsigned)local * (unsigned)(4 * BT);
+                for (unsigned g = g0 + threadIdx.x; g < g0 + 4 * BT && g < ng; g += BT) {
+                    int f = ghost_cell<float>(D.G, a, g);
+                    c0 += f & 1; c1 += (f >> 1) & 1; c2 += (f >> 2) & 1;
+                }
+            }
+            add_counts(c0, c1, c2, a.counters);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (code < 3) atomicAdd(&done[d], 1);
+            else if (code == 3) atomicAdd(&done[ndisc + d], 1);
+        }
+    }
+}
+
+/* CFL reduction over row tiles of every disc: precision-form screening of
+ * setdt_kernel (FP32 cells, FP64 re-evaluation of each tile's winner) */
+__global__ void __launch_bounds__(256)
+batch_setdt_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ tiles, int rows_per_tile)
+{
+    __shared__ MaxLoc sm[8];
+    const uint2 e = tiles[blockIdx.x];
+    const DiscDev &D = discs[e.x];
+    const Geom &G = D.G;
+    const float *V = (const float *)(e.y >> 31 ? D.Vb : D.Va);
+    const int local = (int)(e.y & 0x7fffffffu);
+    const int nj = G.jymax - 2, rows = (G.ixmax - 12) * nj;
+    MaxLoc best = {0.0, -1};
+    for (int r = local * rows_per_tile; r < (local + 1) * rows_per_tile && r < rows; r++) {
+        const int i = 1 + r / nj, j = 1 + r % nj;
+        for (int k = 1 + threadIdx.x; k < G.kzmax - 1; k += blockDim.x) {
+            const long long q = cidx(G, i, j, k), nc = G.nc;
+            float v0 = V[q], v1 = V[nc + q], v2v = V[2 * nc + q], v3 = V[3 * nc + q];
+            float v4 = V[4 * nc + q], v5 = V[5 * nc + q], v6 = V[6 * nc + q], v7 = V[7 * nc + q];
+            float v2 = v1 * v1 + v2v * v2v + v3 * v3;
+            float b2 = v4 * v4 + v5 * v5 + v6 * v6;
+            float t1 = sqrtf(v2 + ((float)MHD_GM * v7 + b2) / v0) / G.f.minlength[(long long)i * G.kzmax + k];
+            int cl = G.cooling ? cooling_rate_f(v0, v7) : 0;
+            float tc = (2.0f * ((v0 * v0 * (float)cl) / (1.5f * v7)));
+            double tmp = (double)rmax<float>(t1, tc);
+            if (tmp > best.v && tmp > 0.0) { best.v = tmp; best.q = q; }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        MaxLoc other;
+        other.v = __shfl_down_sync(0xffffffffu, best.v, o);
+        other.q = __shfl_down_sync(0xffffffffu, best.q, o);
+        best = better(best, other);
+    }
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        MaxLoc b = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = better(b, sm[w]);
+        if (b.q >= 0) {
+            const int k = (int)(b.q % G.kzmax), i = (int)(b.q / ((long long)G.kzmax * G.jymax));
+            b.v = cfl_rate64<float>(G, V, i, b.q, k);
+        }
+        D.part[local] = b;
+    }
+}
+
+/* one block per disc: fold its partials, set its step scalars */
+__global__ void batch_scalars_kernel(const DiscDev *__restrict__ discs)
+{
+    __shared__ MaxLoc sm[32];
+    const DiscDev &D = discs[blockIdx.x];
+    MaxLoc best = {0.0, -1};
+    for (int b = threadIdx.x; b < D.ndt; b += blockDim.x) best = better(best, D.part[b]);
+    for (int o = 16; o > 0; o >>= 1) {
+        MaxLoc x;
+        x.v = __shfl_down_sync(0xffffffffu, best.v, o);
+        x.q = __shfl_down_sync(0xffffffffu, best.q, o);
+        best = better(best, x);
+    }
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) best = better(best, sm[w]);
+    StepScalars *sc = D.sc;
+    if (sc->dtbad) return;
+    double oneocfldt = best.q >= 0 ? best.v : 0.0;
+    double dt = D.cfl / oneocfldt, ch = D.minminlength * oneocfldt;
+    sc->oneocfldt = oneocfldt;
+    sc->argmax = best.q;
+    if (isinf(dt) || dt < D.dtmin) { sc->dtbad = 1; return; }
+    double t = sc->t;
+    double sw = (t - D.tausp) / fabs(t - D.tausp);
+    sc->epssp = 0.5 * D.epssp0 * (t / D.tausp * (1.0 - sw) + (1.0 + sw));
+    sc->dt = dt;
+    sc->ch = ch;
+    sc->psicoef = exp(-dt * ch * MHD_ONEOCR * D.psifac);
+    sc->dtf = (float)dt;
+    sc->chf = (float)ch;
+    sc->psif = (float)sc->psicoef;
+}
+
+__global__ void batch_trig_kernel(const DiscDev *__restrict__ discs)
+{
+    const DiscDev &D = discs[blockIdx.y];
+    if (!D.gravity || D.sc->dtbad) return;
+    const Geom &G = D.G;
+    const int n = G.ixmax * G.jymax;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        int i = q / G.jymax, j = q % G.jymax;
+        double phase = D.armnum * (G.y[j] - D.omdiff * D.sc->t + G.spL[i]);
+        double s, c;
+        sincos(phase, &s, &c);
+        D.trig[q] = c;
+        D.trig[n + q] = s;
+    }
+}
+
+__global__ void batch_advance_kernel(const DiscDev *__restrict__ discs, int ndisc)
+{
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d < ndisc && !discs[d].sc->dtbad) discs[d].sc->t += discs[d].sc->dt;
+}
+
+}  /* namespace */
 
 struct mhd_batch {
-    int n;
+    int n, persistent, nst;
+    cudaStream_t st;
     std::vector<mhd_ctx *> ctx;
     std::vector<int> stopped;
+    std::vector<DiscDev> hd;
+    DiscDev *dd;
+    TileCfg cfg;
+    int nblk_stage;
+    /* tile tables */
+    uint2 *dtiles, *ddt;
+    int ntiles, ndt_tiles, rows_per_tile;
+    int *dqueue;    /* [3 stages]: head ; then done [3 stages][2*n] */
+    int *derr;
+    int *dcnt;      /* per disc [3][3] */
+    cudaGraphExec_t gx[2];
+    int graph_ready, parity;
+    long long launches;
 };
+
+#define BCK(call)                                                                          \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) return e_ == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; \
+    } while (0)
+
+static int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+/* tile tables for a configuration */
+static int build_tiles(mhd_batch *b, TileCfg c)
+{
+    std::vector<uint2> tl;
+    const int n = b->n;
+    for (int d = 0; d < n; d++) {
+        DiscDev &D = b->hd[d];
+        D.nflux = 0;
+        for (int dir = 0; dir < 3; dir++) {
+            const Box &bx = D.fbox[dir];
+            D.ft[dir][0] = ceil_div(bx.i1 - bx.i0, c.ti);
+            D.ft[dir][1] = ceil_div(bx.j1 - bx.j0, c.tj);
+            D.ft[dir][2] = ceil_div(bx.k1 - bx.k0, c.tk);
+            int nt = D.ft[dir][0] * D.ft[dir][1] * D.ft[dir][2];
+            for (int l = 0; l < nt; l++) tl.push_back(make_uint2(d, ((unsigned)dir << 28) | (unsigned)l));
+            D.nflux += nt;
+        }
+    }
+    for (int d = 0; d < n; d++) {
+        DiscDev &D = b->hd[d];
+        D.ut[0] = ceil_div(D.ubox.i1 - D.ubox.i0, c.ti);
+        D.ut[1] = ceil_div(D.ubox.j1 - D.ubox.j0, c.tj);
+        D.ut[2] = ceil_div(D.ubox.k1 - D.ubox.k0, c.tk);
+        D.nupd = D.ut[0] * D.ut[1] * D.ut[2];
+        for (int l = 0; l < D.nupd; l++) tl.push_back(make_uint2(d, (3u << 28) | (unsigned)l));
+    }
+    for (int d = 0; d < n; d++) {
+        DiscDev &D = b->hd[d];
+        long long ng = 2LL * D.G.ixmax * D.G.jymax + 2LL * D.G.ixmax * (D.G.kzmax - 2) +
+                       2LL * (D.G.jymax - 2) * (D.G.kzmax - 2);
+        D.nghost = (int)((ng + 4 * c.bt - 1) / (4 * c.bt));
+        for (int l = 0; l < D.nghost; l++) tl.push_back(make_uint2(d, (4u << 28) | (unsigned)l));
+    }
+    if (b->dtiles) cudaFree(b->dtiles);
+    b->dtiles = NULL;
+    b->ntiles = (int)tl.size();
+    BCK(cudaMalloc((void **)&b->dtiles, tl.size() * sizeof(uint2)));
+    BCK(cudaMemcpy(b->dtiles, tl.data(), tl.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy(b->dd, b->hd.data(), n * sizeof(DiscDev), cudaMemcpyHostToDevice));
+    b->cfg = c;
+    return MHD_OK;
+}
+
+static int stage_blocks(TileCfg c)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    switch (c.variant) {
+    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<128, 4>, 128, 0); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<128, 8>, 128, 0); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<256, 2>, 256, 0); break;
+    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<256, 4>, 256, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<64, 8>, 64, 0); break;
+    }
+    if (per < 1) per = 1;
+    return sms * per;
+}
+
+static cudaError_t launch_stage(mhd_batch *b, int *head, int *done, int kind, int last, int parity, int stage)
+{
+    TileCfg c = b->cfg;
+    int nb = b->nblk_stage;
+#define MHD_STAGE(BT, MB)                                                                                    \
+    batch_stage_kernel<BT, MB><<<nb, BT, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, done, b->n, b->derr, \
+                                                       kind, last, parity, stage, c)
+    switch (c.variant) {
+    case 0: MHD_STAGE(128, 4); break;
+    case 1: MHD_STAGE(128, 8); break;
+    case 2: MHD_STAGE(256, 2); break;
+    case 3: MHD_STAGE(256, 4); break;
+    default: MHD_STAGE(64, 8); break;
+    }
+#undef MHD_STAGE
+    return cudaGetLastError();
+}
+
+/* the launches of one step of all discs, starting at primitive parity `parity` */
+static int enqueue_batch_step(mhd_batch *b, int parity)
+{
+    const int n = b->n;
+    BCK(cudaMemsetAsync(b->dcnt, 0, 9 * n * sizeof(int), b->st));
+    batch_setdt_kernel<<<b->ndt_tiles, 256, 0, b->st>>>(b->dd, parity ? b->ddt + b->ndt_tiles : b->ddt,
+                                                         b->rows_per_tile);
+    BCK(cudaGetLastError());
+    batch_scalars_kernel<<<n, 256, 0, b->st>>>(b->dd);
+    BCK(cudaGetLastError());
+    batch_trig_kernel<<<dim3(64, n), 128, 0, b->st>>>(b->dd);
+    BCK(cudaGetLastError());
+    b->launches += 3;
+    static const int rk3[3][2] = {{0, 0}, {1, 0}, {2, 1}};
+    static const int rk2[2][2] = {{0, 0}, {3, 1}};
+    int par = parity;
+    for (int s = 0; s < b->nst; s++) {
+        int kind = b->nst == 2 ? rk2[s][0] : rk3[s][0], last = b->nst == 2 ? rk2[s][1] : rk3[s][1];
+        int *q = b->dqueue + s * (1 + 2 * n);
+        BCK(cudaMemsetAsync(q, 0, (1 + 2 * n) * sizeof(int), b->st));
+        BCK(launch_stage(b, q, q + 1, kind, last, par, s));
+        b->launches++;
+        par ^= 1;
+    }
+    batch_advance_kernel<<<ceil_div(n, 128), 128, 0, b->st>>>(b->dd, n);
+    BCK(cudaGetLastError());
+    b->launches++;
+    return MHD_OK;
+}
+
+static int build_graphs(mhd_batch *b)
+{
+    for (int q = 0; q < 2; q++) {
+        if (b->gx[q]) cudaGraphExecDestroy(b->gx[q]);
+        b->gx[q] = NULL;
+    }
+    long long l0 = b->launches;
+    for (int par = 0; par < 2; par++) {
+        cudaGraph_t g;
+        BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_batch_step(b, par);
+        cudaError_t e = cudaStreamEndCapture(b->st, &g);
+        if (rc) return rc;
+        BCK(e);
+        BCK(cudaGraphInstantiate(&b->gx[par], g, 0));
+        cudaGraphDestroy(g);
+    }
+    b->launches = l0;
+    b->graph_ready = 1;
+    return MHD_OK;
+}
+
+static int setup_persistent(mhd_batch *b)
+{
+    const int n = b->n;
+    b->hd.assign(n, DiscDev());
+    int maxrows = 0;
+    for (int d = 0; d < n; d++) {
+        mhd_ctx *c = b->ctx[d];
+        DiscDev &D = b->hd[d];
+        memset((void *)&D, 0, sizeof D);
+        D.G = c->G;
+        D.U = (float *)c->U; D.U1 = (float *)c->U1; D.Va = (float *)c->Va; D.Vb = (float *)c->Vb;
+        D.Uinit = (float *)c->Uinit; D.Vinit = (float *)c->Vinit; D.rhofloor = (float *)c->rhofloor;
+        D.F = (float *)c->F; D.Gf = (float *)c->Gf; D.H = (float *)c->H; D.Uraw = (float *)c->Uraw;
+        D.sc = c->d_sc; D.trig = c->d_trig; D.part = c->d_part;
+        for (int dir = 0; dir < 3; dir++) {
+            Box &bx = D.fbox[dir];
+            bx.i0 = dir == 0 ? 0 : 1; bx.i1 = c->ixmax - 1;
+            bx.j0 = dir == 1 ? 0 : 1; bx.j1 = c->jymax - 1;
+            bx.k0 = dir == 2 ? 0 : 1; bx.k1 = c->kzmax - 1;
+        }
+        D.ubox.i0 = 1; D.ubox.i1 = c->ixmax - 1; D.ubox.j0 = 1; D.ubox.j1 = c->jymax - 1;
+        D.ubox.k0 = 1; D.ubox.k1 = c->kzmax - 1;
+        D.cfl = c->p.cfl; D.minminlength = c->G.minminlength; D.dtmin = c->p.dtmin;
+        D.psifac = c->p.scheme == MHD_SCHEME_RK2 ? 0.5 : MHD_ONEO3;
+        D.tausp = c->p.tausp; D.epssp0 = c->p.epssp0; D.omdiff = c->omdiff; D.armnum = (double)c->p.armnum;
+        D.gravity = c->p.gravity;
+        int rows = (c->ixmax - 12) * (c->jymax - 2);
+        if (rows > maxrows) maxrows = rows;
+    }
+    /* CFL row tiles: at most the context's partial buffer per disc */
+    b->rows_per_tile = 8;
+    std::vector<uint2> dt;
+    for (int d = 0; d < n; d++) {
+        mhd_ctx *c = b->ctx[d];
+        int rows = (c->ixmax - 12) * (c->jymax - 2);
+        int rpt = b->rows_per_tile;
+        while (ceil_div(rows, rpt) > c->npart) rpt *= 2;
+        if (rpt > b->rows_per_tile) b->rows_per_tile = rpt;
+    }
+    for (int d = 0; d < n; d++) {
+        mhd_ctx *c = b->ctx[d];
+        int rows = (c->ixmax - 12) * (c->jymax - 2);
+        b->hd[d].ndt = ceil_div(rows, b->rows_per_tile);
+    }
+    for (int par = 0; par < 2; par++)
+        for (int d = 0; d < n; d++)
+            for (int l = 0; l < b->hd[d].ndt; l++)
+                dt.push_back(make_uint2(d, ((unsigned)par << 31) | (unsigned)l));
+    b->ndt_tiles = (int)dt.size() / 2;
+    BCK(cudaMalloc((void **)&b->ddt, dt.size() * sizeof(uint2)));
+    BCK(cudaMemcpy(b->ddt, dt.data(), dt.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    BCK(cudaMalloc((void **)&b->dd, n * sizeof(DiscDev)));
+    BCK(cudaMalloc((void **)&b->dqueue, 3 * (1 + 2 * n) * sizeof(int)));
+    BCK(cudaMalloc((void **)&b->derr, sizeof(int)));
+    BCK(cudaMemset(b->derr, 0, sizeof(int)));
+    BCK(cudaMalloc((void **)&b->dcnt, 9 * n * sizeof(int)));
+    for (int d = 0; d < n; d++) b->hd[d].counters = b->dcnt + 9 * d;
+    BCK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    int rc = build_tiles(b, CANDIDATES[0]);
+    if (rc) return rc;
+    b->nblk_stage = stage_blocks(b->cfg);
+    return MHD_OK;
+}
 
 extern "C" int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *params, mhd_batch **out)
 {
@@ -26,8 +512,22 @@ extern "C" int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *
     b->n = n;
     b->ctx.assign(n, NULL);
     b->stopped.assign(n, 0);
+    int fp32 = params[0].precision == MHD_PREC_FP32;
+    b->nst = params[0].scheme == MHD_SCHEME_RK2 ? 2 : 3;
     for (int i = 0; i < n; i++) {
+        if ((params[i].precision == MHD_PREC_FP32) != fp32 || params[i].scheme != params[0].scheme) {
+            mhd_batch_destroy(b);
+            return MHD_ERR_ARG;   /* one precision and one RK scheme per batch */
+        }
         int rc = mhd_create(&grids[i], &params[i], &b->ctx[i]);
+        if (rc) {
+            mhd_batch_destroy(b);
+            return rc;
+        }
+    }
+    b->persistent = fp32;
+    if (fp32) {
+        int rc = setup_persistent(b);
         if (rc) {
             mhd_batch_destroy(b);
             return rc;
@@ -40,6 +540,13 @@ extern "C" int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *
 extern "C" void mhd_batch_destroy(mhd_batch *b)
 {
     if (!b) return;
+    if (b->st) cudaStreamSynchronize(b->st);
+    for (int q = 0; q < 2; q++)
+        if (b->gx[q]) cudaGraphExecDestroy(b->gx[q]);
+    void *p[] = {b->dd, b->dtiles, b->ddt, b->dqueue, b->derr, b->dcnt};
+    for (size_t q = 0; q < sizeof p / sizeof p[0]; q++)
+        if (p[q]) cudaFree(p[q]);
+    if (b->st) cudaStreamDestroy(b->st);
     for (mhd_ctx *c : b->ctx)
         if (c) mhd_destroy(c);
     delete b;
@@ -49,19 +556,65 @@ extern "C" int mhd_batch_upload(mhd_batch *b, int disc, const double *U, const d
                                 const double *Vinit, const double *rhofloor)
 {
     if (!b || disc < 0 || disc >= b->n) return MHD_ERR_ARG;
+    if (b->st) BCK(cudaStreamSynchronize(b->st));
     b->stopped[disc] = 0;
-    return mhd_upload(b->ctx[disc], U, V, Uinit, Vinit, rhofloor);
+    int rc = mhd_upload(b->ctx[disc], U, V, Uinit, Vinit, rhofloor);
+    if (rc) return rc;
+    /* all discs share the batch's primitive parity */
+    if (b->persistent && b->parity) {
+        mhd_ctx *c = b->ctx[disc];
+        BCK(cudaMemcpy(c->Vb, c->Va, 9 * c->nc * sizeof(float), cudaMemcpyDeviceToDevice));
+        c->vcur = 1;
+    }
+    return MHD_OK;
 }
 
 extern "C" int mhd_batch_download(mhd_batch *b, int disc, double *U, double *V)
 {
     if (!b || disc < 0 || disc >= b->n) return MHD_ERR_ARG;
+    if (b->st) BCK(cudaStreamSynchronize(b->st));
     return mhd_download(b->ctx[disc], U, V);
+}
+
+static int batch_run(mhd_batch *b, int nsteps, double *t, int *status)
+{
+    const int n = b->n;
+    for (int d = 0; d < n; d++) {
+        StepScalars *h = b->ctx[d]->h_sc;
+        h->t = t[d];
+        h->dtbad = b->stopped[d];
+        BCK(cudaMemcpyAsync(b->ctx[d]->d_sc, h, sizeof(StepScalars), cudaMemcpyHostToDevice, b->st));
+    }
+    BCK(cudaMemsetAsync(b->derr, 0, sizeof(int), b->st));
+    if (!b->graph_ready) {
+        int rc = build_graphs(b);
+        if (rc) return rc;
+    }
+    long long per_step = 3 + b->nst + 1;
+    for (int s = 0; s < nsteps; s++) {
+        BCK(cudaGraphLaunch(b->gx[b->parity], b->st));
+        b->parity ^= (b->nst & 1);
+        b->launches += per_step;
+    }
+    for (int d = 0; d < n; d++)
+        BCK(cudaMemcpyAsync(b->ctx[d]->h_sc, b->ctx[d]->d_sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, b->st));
+    int herr = 0;
+    BCK(cudaMemcpyAsync(&herr, b->derr, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+    BCK(cudaStreamSynchronize(b->st));
+    for (int d = 0; d < n; d++) {
+        t[d] = b->ctx[d]->h_sc->t;
+        b->ctx[d]->vcur = b->parity;
+        if (b->ctx[d]->h_sc->dtbad) b->stopped[d] = 1;
+    }
+    if (status)
+        for (int d = 0; d < n; d++) status[d] = b->stopped[d] ? MHD_ERR_DT : MHD_OK;
+    return herr ? MHD_ERR_TIMEOUT : MHD_OK;
 }
 
 extern "C" int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status)
 {
     if (!b || !t || nsteps < 0) return MHD_ERR_ARG;
+    if (b->persistent) return batch_run(b, nsteps, t, status);
     for (int s = 0; s < nsteps; s++)
         for (int i = 0; i < b->n; i++) {
             if (b->stopped[i]) continue;
@@ -79,6 +632,68 @@ extern "C" int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status)
 extern "C" int mhd_batch_tune(mhd_batch *b, int *best)
 {
     if (!b || !best) return MHD_ERR_ARG;
-    best[0] = 1; best[1] = 1; best[2] = 128; best[3] = 128;
+    if (!b->persistent) {
+        best[0] = 1; best[1] = 1; best[2] = 128; best[3] = 128;
+        return MHD_OK;
+    }
+    const int n = b->n;
+    BCK(cudaStreamSynchronize(b->st));
+    /* snapshot the evolving state */
+    std::vector<std::vector<double>> U(n), V(n);
+    std::vector<double> t0(n), tt(n);
+    std::vector<int> stop0 = b->stopped;
+    int par0 = b->parity;
+    for (int d = 0; d < n; d++) {
+        mhd_ctx *c = b->ctx[d];
+        U[d].resize(9 * c->nc);
+        V[d].resize(9 * c->nc);
+        int rc = mhd_download(c, U[d].data(), V[d].data());
+        if (rc) return rc;
+        t0[d] = c->h_sc->t;
+    }
+    auto restore = [&]() -> int {
+        b->parity = 0;
+        for (int d = 0; d < n; d++) {
+            int rc = mhd_upload_state(b->ctx[d], U[d].data(), V[d].data());
+            if (rc) return rc;
+            b->ctx[d]->vcur = 0;
+        }
+        b->stopped = stop0;
+        return MHD_OK;
+    };
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    int best_i = 0;
+    for (int ci = 0; ci < NCAND; ci++) {
+        int rc = restore();
+        if (rc) return rc;
+        if ((rc = build_tiles(b, CANDIDATES[ci]))) return rc;
+        b->nblk_stage = stage_blocks(b->cfg);
+        b->graph_ready = 0;
+        tt = t0;
+        if ((rc = batch_run(b, 1, tt.data(), NULL))) return rc;   /* warm-up + graph build */
+        BCK(cudaEventRecord(e0, b->st));
+        if ((rc = batch_run(b, 3, tt.data(), NULL))) return rc;
+        BCK(cudaEventRecord(e1, b->st));
+        BCK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        BCK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) { best_ms = ms; best_i = ci; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int rc = restore();
+    if (rc) return rc;
+    for (int d = 0; d < n; d++) b->ctx[d]->h_sc->t = t0[d];
+    if ((rc = build_tiles(b, CANDIDATES[best_i]))) return rc;
+    b->nblk_stage = stage_blocks(b->cfg);
+    b->graph_ready = 0;
+    (void)par0;
+    best[0] = CANDIDATES[best_i].ti;
+    best[1] = CANDIDATES[best_i].tj;
+    best[2] = CANDIDATES[best_i].tk;
+    best[3] = CANDIDATES[best_i].bt;
     return MHD_OK;
 }

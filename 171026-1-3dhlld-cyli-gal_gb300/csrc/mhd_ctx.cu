@@ -22,48 +22,11 @@
 
 #include <vector>
 
-#include "mhd_launch.h"
+#include "mhd_ctx_internal.h"
 
 using namespace mhd;
 
-struct mhd_ctx {
-    int device;
-    cudaStream_t st;
-    mhd_params p;
-    int ix, jy, kz, ixmax, jymax, kzmax, irin;
-    long long nc;
-    int fp32;
-    size_t esz;
-    Geom G;
-    double *dtab;
-    float *ftab;
-    void *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
-    int vcur;
-    StepScalars *d_sc, *h_sc;
-    double *d_trig, *h_trig;
-    MaxLoc *d_part, *h_part;
-    int npart;
-    int *d_cnt, *h_cnt;
-    double *d_stage;
-    long long stage_n;
-    std::vector<double> hx, hy, hspL;
-    double omdiff;
-    int uploaded;
-    cudaError_t last_cuda;
-    /* mhd_run graph */
-    cudaGraphExec_t gexec;
-    cudaGraphExec_t gexecs[2];
-    int graph_ready, graph_launches;
-    int *d_cnt_run;
-    /* instrumentation */
-    long long launches;
-    int prof, nslot;
-    cudaEvent_t ev[2 * 256];
-    int slot_kind[256];
-    double prof_ms[MHD_PROF_NKIND];
-    long long prof_n[MHD_PROF_NKIND];
-    cudaEvent_t tev[2];
-};
+
 
 enum { PK_FLUX_R = 0, PK_FLUX_PHI = 1, PK_FLUX_Z = 2, PK_UPDATE = 3, PK_GHOST = 4, PK_SETDT = 5, PK_TRIG = 6,
        PK_CVT = 7 };

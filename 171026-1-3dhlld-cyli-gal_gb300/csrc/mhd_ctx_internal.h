@@ -1,0 +1,53 @@
+/*
+ * mhd_ctx_internal.h -- the context object behind the C-ABI, shared by the
+ * context code (mhd_ctx.cu) and the batched form (mhd_batch.cu).
+ */
+#ifndef MHD_CTX_INTERNAL_H
+#define MHD_CTX_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "mhd_launch.h"
+
+struct mhd_ctx {
+    int device;
+    cudaStream_t st;
+    mhd_params p;
+    int ix, jy, kz, ixmax, jymax, kzmax, irin;
+    long long nc;
+    int fp32;
+    size_t esz;
+    mhd::Geom G;
+    double *dtab;
+    float *ftab;
+    void *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
+    int vcur;
+    mhd::StepScalars *d_sc, *h_sc;
+    double *d_trig, *h_trig;
+    mhd::MaxLoc *d_part, *h_part;
+    int npart;
+    int *d_cnt, *h_cnt;
+    double *d_stage;
+    long long stage_n;
+    std::vector<double> hx, hy, hspL;
+    double omdiff;
+    int uploaded;
+    cudaError_t last_cuda;
+    /* mhd_run graph */
+    cudaGraphExec_t gexec;
+    cudaGraphExec_t gexecs[2];
+    int graph_ready, graph_launches;
+    int *d_cnt_run;
+    /* instrumentation */
+    long long launches;
+    int prof, nslot;
+    cudaEvent_t ev[2 * 256];
+    int slot_kind[256];
+    double prof_ms[MHD_PROF_NKIND];
+    long long prof_n[MHD_PROF_NKIND];
+    cudaEvent_t tev[2];
+};
+
+#endif

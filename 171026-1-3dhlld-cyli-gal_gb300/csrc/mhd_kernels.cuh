@@ -26,15 +26,11 @@ namespace mhd {
 /* ------------------------------------------------------------------------ */
 /* fluxes                                                                    */
 /* ------------------------------------------------------------------------ */
+/* one face: reconstruction of the two adjacent cells, Riemann + GLM flux */
 template <typename T, int DIR, bool REFLAYOUT>
-__global__ void __launch_bounds__(128)
-flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
-            T *__restrict__ F, Box b)
+__device__ __forceinline__ void flux_face(const Geom &G, const T *__restrict__ V, const T *__restrict__ Vinit,
+                                          const StepScalars *__restrict__ sc, T *__restrict__ F, int i, int j, int k)
 {
-    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = b.j0 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = b.i0 + blockIdx.z;
-    if (k >= b.k1 || j >= b.j1) return;
     T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
     T L[9], R[9], Fo[9];
     face_states<T, DIR>(G, V, Vinit, i, j, k, dt, psicoef, L, R);
@@ -50,6 +46,18 @@ flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const 
 #pragma unroll
         for (int m = 0; m < 9; m++) F[m * G.nc + q] = Fo[m];
     }
+}
+
+template <typename T, int DIR, bool REFLAYOUT>
+__global__ void __launch_bounds__(128)
+flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
+            T *__restrict__ F, Box b)
+{
+    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = b.j0 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = b.i0 + blockIdx.z;
+    if (k >= b.k1 || j >= b.j1) return;
+    flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, i, j, k);
 }
 
 /* reconstructed face states in the reference's face layout (probe) */
@@ -108,55 +116,63 @@ __device__ __forceinline__ void absorb(const Geom &G, const T *__restrict__ Uini
 /* kind: 0 U1=U-dtL (Halfstep/FirstStep), 1 U1=(3U+U1-dtL)/4 (SecondStep),
  *       2 U=(U+2(U1-dtL))/3 (ThirdStep), 3 U=(U+U1-dtL)/2 (Fullstep) */
 template <typename T>
-__global__ void __launch_bounds__(128)
-update_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ F, const T *__restrict__ Gf,
-              const T *__restrict__ H, T *Un, T *U1, const T *__restrict__ Uinit,
-              const T *__restrict__ rhofloor, T *__restrict__ Vout, T *__restrict__ Uraw,
-              const StepScalars *__restrict__ sc, const double *__restrict__ trig, int kind, int last,
-              int *counters)
+__device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a, int i, int j, int k)
 {
-    if (sc->dtbad) return;
+    const Tabs<T> &tb = tabs<T>(G);
+    const StepScalars *sc = a.sc;
+    const long long nc = G.nc, q = cidx(G, i, j, k);
+    const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
+    const long long gk = (long long)i * G.kzmax + k, pl = (long long)G.ixmax * G.kzmax;
+    const T g1 = tb.g[gk], g2 = tb.g[pl + gk], g3 = tb.g[2 * pl + gk];
+    const T g4 = tb.g[3 * pl + gk], g5 = tb.g[4 * pl + gk], g6 = tb.g[5 * pl + gk];
+    const T dt = Scal<T>::dt(sc), psicoef = Scal<T>::psi(sc);
+    const T *__restrict__ V = a.V;
+    const T *__restrict__ F = a.F;
+    const T *__restrict__ Gf = a.G;
+    const T *__restrict__ H = a.H;
+    const int kind = a.kind;
+    T W[9], S[9], u[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) W[m] = V[m * nc + q];
+    source_at<T>(G, *sc, a.trig, i, j, k, W, S);
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+        const long long mq = m * nc + q;
+        T div = ((g2 * F[mq] - g1 * F[mq - si]) + (g4 * Gf[mq] - g3 * Gf[mq - sj]) + (g6 * H[mq] - g5 * H[mq - 1]));
+        T un = a.Un[mq], u1 = (kind == 0) ? T(0) : a.U1[mq];
+        if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
+        T v;
+        if (kind == 0) v = un - dt * div + dt * S[m];
+        else if (kind == 1) v = T(0.25) * (T(3.0) * un + u1 - dt * div + dt * S[m]);
+        else if (kind == 2) v = T(MHD_ONEO3) * (un + T(2.0) * (u1 - dt * div + dt * S[m]));
+        else v = T(0.5) * (un + u1 - dt * div + dt * S[m]);
+        u[m] = v;
+    }
+    if (is_bc_source(G, i, j, k)) {
+#pragma unroll
+        for (int m = 0; m < 9; m++) a.Uraw[m * nc + q] = u[m];
+    }
+    if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);   /* zboundary.h:87 */
+    if (a.last) absorb<T>(G, a.Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
+    int flags = utov_check<T>(G, i, a.rhofloor[q], u, W);
+    T *Uo = (kind == 0 || kind == 1) ? a.U1 : a.Un;
+#pragma unroll
+    for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; a.Vout[m * nc + q] = W[m]; }
+    return flags;
+}
+
+/* kind: 0 U1=U-dtL (Halfstep/FirstStep), 1 U1=(3U+U1-dtL)/4 (SecondStep),
+ *       2 U=(U+2(U1-dtL))/3 (ThirdStep), 3 U=(U+U1-dtL)/2 (Fullstep) */
+template <typename T>
+__global__ void __launch_bounds__(128) update_kernel(Geom G, StageArgs<T> a)
+{
+    if (a.sc->dtbad) return;
     const int k = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
     const int i = 1 + blockIdx.z;
     int flags = 0;
-    if (k < G.kzmax - 1 && j < G.jymax - 1) {
-        const Tabs<T> &tb = tabs<T>(G);
-        const long long nc = G.nc, q = cidx(G, i, j, k);
-        const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
-        const long long gk = (long long)i * G.kzmax + k, pl = (long long)G.ixmax * G.kzmax;
-        const T g1 = tb.g[gk], g2 = tb.g[pl + gk], g3 = tb.g[2 * pl + gk];
-        const T g4 = tb.g[3 * pl + gk], g5 = tb.g[4 * pl + gk], g6 = tb.g[5 * pl + gk];
-        const T dt = Scal<T>::dt(sc), psicoef = Scal<T>::psi(sc);
-        T W[9], S[9], u[9];
-#pragma unroll
-        for (int m = 0; m < 9; m++) W[m] = V[m * nc + q];
-        source_at<T>(G, *sc, trig, i, j, k, W, S);
-#pragma unroll
-        for (int m = 0; m < 9; m++) {
-            const long long mq = m * nc + q;
-            T div = ((g2 * F[mq] - g1 * F[mq - si]) + (g4 * Gf[mq] - g3 * Gf[mq - sj]) + (g6 * H[mq] - g5 * H[mq - 1]));
-            T un = Un[mq], u1 = (kind == 0) ? T(0) : U1[mq];
-            if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
-            T v;
-            if (kind == 0) v = un - dt * div + dt * S[m];
-            else if (kind == 1) v = T(0.25) * (T(3.0) * un + u1 - dt * div + dt * S[m]);
-            else if (kind == 2) v = T(MHD_ONEO3) * (un + T(2.0) * (u1 - dt * div + dt * S[m]));
-            else v = T(0.5) * (un + u1 - dt * div + dt * S[m]);
-            u[m] = v;
-        }
-        if (is_bc_source(G, i, j, k)) {
-#pragma unroll
-            for (int m = 0; m < 9; m++) Uraw[m * nc + q] = u[m];
-        }
-        if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);   /* zboundary.h:87 */
-        if (last) absorb<T>(G, Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
-        flags = utov_check<T>(G, i, rhofloor[q], u, W);
-        T *Uo = (kind == 0 || kind == 1) ? U1 : Un;
-#pragma unroll
-        for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; Vout[m * nc + q] = W[m]; }
-    }
-    add_counters(flags, counters);
+    if (k < G.kzmax - 1 && j < G.jymax - 1) flags = update_cell<T>(G, a, i, j, k);
+    add_counters(flags, a.counters);
 }
 
 /* Ghost cell -> (source interior cell, sign flip mask) after the fill sequence
@@ -189,53 +205,68 @@ __device__ __forceinline__ void ghost_source(const Geom &G, int i, int j, int k,
     else if (j == G.jymax - 1) sj = 1;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(128)
-ghost_kernel(Geom G, const T *__restrict__ Uraw, T *Uo, const T *__restrict__ Uinit,
-             const T *__restrict__ rhofloor, T *__restrict__ Vout, const StepScalars *__restrict__ sc,
-             int last, int *counters)
+/* number of ghost cells and the ghost cell with enumeration index tid:
+ * k planes (k=0, kzmax-1), then j planes, then i planes */
+__device__ __forceinline__ unsigned ghost_count(const Geom &G)
 {
-    if (sc->dtbad) return;
-    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
+    return 2 * ni * nj + 2 * ni * (nk - 2) + 2 * (nj - 2) * (nk - 2);
+}
+
+__device__ __forceinline__ void ghost_cell_of(const Geom &G, unsigned tid, int &i, int &j, int &k)
+{
     const unsigned nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
     const unsigned nkplane = 2 * ni * nj;
     const unsigned njplane = 2 * ni * (nk - 2);
-    const unsigned niplane = 2 * (nj - 2) * (nk - 2);
-    int flags = 0;
-    if (tid < nkplane + njplane + niplane) {
-        int i, j, k;
-        if (tid < nkplane) {
-            k = (tid < ni * nj) ? 0 : (int)nk - 1;
-            unsigned r = tid % (ni * nj);
-            i = (int)(r / nj); j = (int)(r % nj);
-        } else if (tid < nkplane + njplane) {
-            unsigned r = tid - nkplane;
-            j = (r < ni * (nk - 2)) ? 0 : (int)nj - 1;
-            r %= ni * (nk - 2);
-            i = (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
-        } else {
-            unsigned r = tid - nkplane - njplane;
-            i = (r < (nj - 2) * (nk - 2)) ? 0 : (int)ni - 1;
-            r %= (nj - 2) * (nk - 2);
-            j = 1 + (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
-        }
-        int si, sj, sk;
-        unsigned neg;
-        ghost_source(G, i, j, k, si, sj, sk, neg);
-        const long long nc = G.nc, q = cidx(G, i, j, k), qs = cidx(G, si, sj, sk);
-        T u[9], W[9];
-#pragma unroll
-        for (int m = 0; m < 9; m++) {
-            T v = Uraw[m * nc + qs];
-            u[m] = ((neg >> m) & 1u) ? -v : v;
-        }
-        if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);
-        if (last) absorb<T>(G, Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
-        flags = utov_check<T>(G, i, rhofloor[q], u, W);
-#pragma unroll
-        for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; Vout[m * nc + q] = W[m]; }
+    if (tid < nkplane) {
+        k = (tid < ni * nj) ? 0 : (int)nk - 1;
+        unsigned r = tid % (ni * nj);
+        i = (int)(r / nj); j = (int)(r % nj);
+    } else if (tid < nkplane + njplane) {
+        unsigned r = tid - nkplane;
+        j = (r < ni * (nk - 2)) ? 0 : (int)nj - 1;
+        r %= ni * (nk - 2);
+        i = (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
+    } else {
+        unsigned r = tid - nkplane - njplane;
+        i = (r < (nj - 2) * (nk - 2)) ? 0 : (int)ni - 1;
+        r %= (nj - 2) * (nk - 2);
+        j = 1 + (int)(r / (nk - 2)); k = 1 + (int)(r % (nk - 2));
     }
-    add_counters(flags, counters);
+}
+
+template <typename T>
+__device__ __forceinline__ int ghost_cell(const Geom &G, const StageArgs<T> &a, unsigned tid)
+{
+    int i, j, k;
+    ghost_cell_of(G, tid, i, j, k);
+    int si, sj, sk;
+    unsigned neg;
+    ghost_source(G, i, j, k, si, sj, sk, neg);
+    const long long nc = G.nc, q = cidx(G, i, j, k), qs = cidx(G, si, sj, sk);
+    T u[9], W[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+        T v = a.Uraw[m * nc + qs];
+        u[m] = ((neg >> m) & 1u) ? -v : v;
+    }
+    if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);
+    if (a.last) absorb<T>(G, a.Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
+    int flags = utov_check<T>(G, i, a.rhofloor[q], u, W);
+    T *Uo = (a.kind == 0 || a.kind == 1) ? a.U1 : a.Un;
+#pragma unroll
+    for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; a.Vout[m * nc + q] = W[m]; }
+    return flags;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) ghost_kernel(Geom G, StageArgs<T> a)
+{
+    if (a.sc->dtbad) return;
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    int flags = 0;
+    if (tid < ghost_count(G)) flags = ghost_cell<T>(G, a, tid);
+    add_counters(flags, a.counters);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -405,8 +436,7 @@ cudaError_t launch_update_t(const Geom &G, const StageArgs<T> &a, cudaStream_t s
 {
     dim3 gr, bl;
     grid3(G.kzmax - 2, G.jymax - 2, G.ixmax - 2, gr, bl);
-    update_kernel<T><<<gr, bl, 0, st>>>(G, a.V, a.F, a.G, a.H, a.Un, a.U1, a.Uinit, a.rhofloor,
-                                                      a.Vout, a.Uraw, a.sc, a.trig, a.kind, a.last, a.counters);
+    update_kernel<T><<<gr, bl, 0, st>>>(G, a);
     return cudaGetLastError();
 }
 
@@ -414,9 +444,7 @@ template <typename T>
 cudaError_t launch_ghost_t(const Geom &G, const StageArgs<T> &a, cudaStream_t st)
 {
     long long ng = 2LL * G.ixmax * G.jymax + 2LL * G.ixmax * (G.kzmax - 2) + 2LL * (G.jymax - 2) * (G.kzmax - 2);
-    T *Uo = (a.kind == 0 || a.kind == 1) ? a.U1 : a.Un;
-    ghost_kernel<T><<<nblocks(ng, 128), 128, 0, st>>>(G, a.Uraw, Uo, a.Uinit, a.rhofloor, a.Vout, a.sc, a.last,
-                                                      a.counters);
+    ghost_kernel<T><<<nblocks(ng, 128), 128, 0, st>>>(G, a);
     return cudaGetLastError();
 }
 

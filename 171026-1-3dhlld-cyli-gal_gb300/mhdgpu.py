@@ -393,3 +393,73 @@ class Disc:
 def pin(a, on=True):
     """page-lock a numpy array's buffer for fast async copies"""
     check(lib().mhd_pin(_ptr(a), a.nbytes, 1 if on else 0), "mhd_pin")
+
+
+# ---------------------------------------------------------------------------
+# batched discs
+# ---------------------------------------------------------------------------
+
+class Batch:
+    """Many independent discs stepped together (mhd_batch_*)."""
+
+    def __init__(self, grids, params):
+        self.grids = list(grids)
+        n = len(self.grids)
+        G = (MhdGrid * n)(*[g.g for g in self.grids])
+        Pp = (MhdParams * n)(*params)
+        h = C.c_void_p()
+        check(lib().mhd_batch_create(n, G, Pp, C.byref(h)), "mhd_batch_create")
+        self.h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().mhd_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    __del__ = close
+
+    def upload(self, d, U, V):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        check(lib().mhd_batch_upload(self.h, d, _ptr(U), _ptr(V), None, None, None), "mhd_batch_upload")
+
+    def download(self, d):
+        g = self.grids[d]
+        U = np.zeros((9,) + g.cell)
+        V = np.zeros((9,) + g.cell)
+        check(lib().mhd_batch_download(self.h, d, _ptr(U), _ptr(V)), "mhd_batch_download")
+        return U, V
+
+    def step(self, nsteps, t):
+        t = np.array(t, dtype=np.float64, copy=True)   # advanced in place by the library
+        st = np.zeros(self.n, dtype=np.int32)
+        check(lib().mhd_batch_step(self.h, int(nsteps), t, st), "mhd_batch_step")
+        return t, st
+
+    def tune(self):
+        best = np.zeros(4, dtype=np.int32)
+        check(lib().mhd_batch_tune(self.h, best), "mhd_batch_tune")
+        return tuple(int(v) for v in best)
+
+
+def batch_workload(n=64, seed=7):
+    """The batched workload: n discs with sizes drawn from seed 7 (nr in
+    {32,64,96,128}, nphi in {64,128,256}, nz in {32,48,64}), beta log-uniform in
+    [1,100], spiral amplitude uniform in [0, 0.05], pattern speed uniform in
+    [0.3, 0.8], per-disc perturbation seed; precision form, HLLD, minmod, RK3,
+    spiral + axisymmetric gravity on, cooling on."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for d in range(n):
+        nr = int(rng.choice([32, 64, 96, 128]))
+        nphi = int(rng.choice([64, 128, 256]))
+        nz = int(rng.choice([32, 48, 64]))
+        beta = float(10 ** rng.uniform(0.0, 2.0))
+        eps = float(rng.uniform(0.0, 0.05))
+        omp = float(rng.uniform(0.3, 0.8))
+        (nr, nphi, nz), params, ic = workload("disc2", nr=nr, nphi=nphi, nz=nz, limiter="minmod",
+                                              precision="fp32", epssp0=eps, omegapattern=omp, beta=beta)
+        ic["seed"] = 1000 + d
+        out.append(((nr, nphi, nz), params, ic))
+    return out

@@ -1,0 +1,122 @@
+"""The batched form: uneven discs in one persistent launch per RK stage.
+
+Each disc of a batch must follow the same trajectory as the same disc stepped
+alone by the device-resident single-disc path (mhd_run) -- the same per-cell
+code, the same device-side dt -- to 1e-6 relative L1, and stay within the
+precision form's tolerance of its own plain FP64 run."""
+import numpy as np
+import pytest
+
+from mhdcase import rel_l1
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(16, 16, 16), (24, 8, 20), (32, 12, 14), (20, 16, 24)]
+
+
+def make_discs(M, fp="fp32", dtmin_bad=None):
+    cases = []
+    for d, dims in enumerate(SIZES):
+        over = dict(precision=fp, epssp0=0.01 * (d + 1), omegapattern=0.3 + 0.1 * d, beta=1.0 + 10 * d,
+                    limiter="minmod" if d % 2 == 0 else "mc")
+        if dtmin_bad is not None and d == dtmin_bad:
+            over["dtmin"] = 1.0e3
+        (nr, nphi, nz), params, ic = M.workload("disc2", nr=dims[0], nphi=dims[1], nz=dims[2], **over)
+        ic["seed"] = 50 + d
+        grid = M.Grid.disc(nr, nphi, nz)
+        grid.set_initial_gravity()
+        U, V = grid.ic_disc(**ic)
+        cases.append((grid, params, U, V))
+    return cases
+
+
+def test_batch_matches_single_disc_runs(M):
+    cases = make_discs(M)
+    b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
+    for d, (g, p, U, V) in enumerate(cases):
+        b.upload(d, U, V)
+    t = np.zeros(len(cases))
+    t, st = b.step(3, t)
+    t, st = b.step(2, t)
+    assert np.all(st == 0)
+    for d, (g, p, U, V) in enumerate(cases):
+        s = M.Disc(g, p)
+        s.upload(U, V)
+        ts = s.run(5, 0.0)
+        Us, _ = s.download()
+        Ub, _ = b.download(d)
+        assert abs(ts - t[d]) <= 1e-12 * ts, d
+        assert np.all(rel_l1(Ub[:8], Us[:8]) <= 1e-6), (d, rel_l1(Ub, Us))
+        s.close()
+    b.close()
+
+
+def test_batch_against_fp64(M):
+    cases = make_discs(M)
+    b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
+    for d, (g, p, U, V) in enumerate(cases):
+        b.upload(d, U, V)
+    t, st = b.step(4, np.zeros(len(cases)))
+    for d, (g, p, U, V) in enumerate(cases):
+        pd = p.as_dict()
+        pd.pop("precision")
+        s = M.Disc(g, M.default_params(precision="fp64", **pd))
+        s.upload(U, V)
+        tt = 0.0
+        for _ in range(4):
+            rc, tt, *_ = s.step(tt)
+        U64, _ = s.download()
+        Ub, _ = b.download(d)
+        assert np.all(rel_l1(Ub[[0, 2, 5, 7]], U64[[0, 2, 5, 7]]) <= 1e-4), (d, rel_l1(Ub, U64))
+        s.close()
+    b.close()
+
+
+def test_batch_per_disc_dt_guard(M):
+    cases = make_discs(M, dtmin_bad=2)
+    b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
+    for d, (g, p, U, V) in enumerate(cases):
+        b.upload(d, U, V)
+    t, st = b.step(3, np.zeros(len(cases)))
+    assert st[2] == M.MHD_ERR_DT and t[2] == 0.0
+    assert all(st[d] == 0 and t[d] > 0 for d in (0, 1, 3))
+    U2, _ = b.download(2)
+    # frozen: the uploaded state as the precision form stores it (FP32)
+    assert np.array_equal(U2, cases[2][2].astype(np.float32).astype(np.float64))
+    b.close()
+
+
+def test_batch_tune_restores_state(M):
+    cases = make_discs(M)
+    b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
+    for d, (g, p, U, V) in enumerate(cases):
+        b.upload(d, U, V)
+    t, st = b.step(2, np.zeros(len(cases)))
+    before = [b.download(d) for d in range(len(cases))]
+    best = b.tune()
+    assert best[3] in (64, 128, 256) and best[2] > 0
+    for d in range(len(cases)):
+        Ua, Va = b.download(d)
+        assert np.array_equal(Ua, before[d][0]) and np.array_equal(Va, before[d][1])
+    t2, st2 = b.step(2, t)
+    assert np.all(st2 == 0) and np.all(t2 > t)
+    b.close()
+
+
+def test_batch_plain_fp64_is_bitwise_per_disc(M):
+    cases = make_discs(M, fp="fp64")[:2]
+    b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
+    for d, (g, p, U, V) in enumerate(cases):
+        b.upload(d, U, V)
+    t, st = b.step(2, np.zeros(2))
+    for d, (g, p, U, V) in enumerate(cases):
+        s = M.Disc(g, p)
+        s.upload(U, V)
+        tt = 0.0
+        for _ in range(2):
+            rc, tt, *_ = s.step(tt)
+        Us, _ = s.download()
+        Ub, _ = b.download(d)
+        assert np.array_equal(Us, Ub)
+        s.close()
+    b.close()
