@@ -41,13 +41,14 @@
 
 using namespace mhd;
 
-namespace {
+namespace mhd_batch_k {
 
 struct DiscDev {
     Geom G;
     float *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
     StepScalars *sc;
     double *trig;
+    float *trigf;
     MaxLoc *part;
     int *counters;          /* [3 stages][3] */
     Box fbox[3], ubox;      /* flux face boxes per direction, interior box */
@@ -62,11 +63,22 @@ struct TileCfg {
     int ti, tj, tk, bt, variant;
 };
 
-/* candidate configurations: tile ti x tj x tk cells, bt threads, launch-bounds
- * variant (register cap 65536/(bt*minblocks)) */
+/* candidate configurations, each a compiled variant: tile ti x tj x tk cells
+ * (512-1024 per queue item, so the queue head sees few atomics), bt threads,
+ * register cap 65536/(bt*minblocks) */
+#define MHD_BATCH_VARIANTS(X)      \
+    X(0, 128, 4, 1, 4, 128)        \
+    X(1, 256, 2, 1, 4, 128)        \
+    X(2, 256, 2, 1, 8, 128)        \
+    X(3, 256, 2, 2, 4, 128)        \
+    X(4, 128, 4, 1, 8, 64)         \
+    X(5, 256, 3, 1, 4, 256)        \
+    X(6, 512, 1, 1, 4, 128)        \
+    X(7, 128, 6, 1, 4, 128)
 static const TileCfg CANDIDATES[] = {
-    {1, 1, 128, 128, 0}, {1, 2, 64, 128, 0}, {1, 4, 32, 128, 0}, {2, 2, 32, 128, 0},
-    {1, 2, 64, 128, 1},  {1, 4, 64, 256, 2}, {1, 2, 128, 256, 3}, {1, 1, 64, 64, 4},
+#define MHD_CAND(V, BT, MB, TI, TJ, TK) {TI, TJ, TK, BT, V},
+    MHD_BATCH_VARIANTS(MHD_CAND)
+#undef MHD_CAND
 };
 static const int NCAND = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
 #define MHD_SPIN_LIMIT (1 << 24)
@@ -101,12 +113,24 @@ __device__ __forceinline__ bool wait_at_least(int *flag, int target, int *err)
     return false;
 }
 
-template <int BT, int MINB>
+/* a block's copy of its disc's geometry: table pointers are then read from
+ * shared memory instead of being kept in registers or reloaded from the
+ * descriptor in global memory */
+__device__ __forceinline__ void load_geom(Geom &sG, const Geom &G)
+{
+    const int *src = (const int *)&G;
+    int *dst = (int *)&sG;
+    for (int w = threadIdx.x; w < (int)(sizeof(Geom) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+}
+
+template <int BT, int MINB, int TI, int TJ, int TK>
 __global__ void __launch_bounds__(BT, MINB)
 batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ tiles, int ntiles, int *head,
-                   int *done, int ndisc, int *err, int kind, int last, int parity, int stage, TileCfg cfg)
+                   int *done, int ndisc, int *err, int kind, int last, int parity, int stage)
 {
     __shared__ int s_t, s_ok;
+    __shared__ Geom sG;
     for (;;) {
         if (threadIdx.x == 0) s_t = atomicAdd(head, 1);
         __syncthreads();
@@ -115,6 +139,7 @@ batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ 
         const uint2 e = tiles[t];
         const int d = (int)e.x, code = (int)(e.y >> 28), local = (int)(e.y & 0x0fffffffu);
         const DiscDev &D = discs[d];
+        load_geom(sG, D.G);
         if (threadIdx.x == 0) {
             int ok = 1;
             if (code == 3) ok = wait_at_least(&done[d], D.nflux, err);
@@ -129,39 +154,40 @@ batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ 
             const Box &b = D.fbox[code];
             const int ntk = D.ft[code][2], ntj = D.ft[code][1];
             const int tk = local % ntk, tj = (local / ntk) % ntj, tii = local / (ntk * ntj);
-            const int n = cfg.ti * cfg.tj * cfg.tk;
+            constexpr int n = TI * TJ * TK;
             float *Fd = code == 0 ? D.F : code == 1 ? D.Gf : D.H;
             for (int c = threadIdx.x; c < n; c += BT) {
-                const int kk = c % cfg.tk, jj = (c / cfg.tk) % cfg.tj, ii = c / (cfg.tk * cfg.tj);
-                const int i = b.i0 + tii * cfg.ti + ii, j = b.j0 + tj * cfg.tj + jj, k = b.k0 + tk * cfg.tk + kk;
+                const int kk = c % TK, jj = (c / TK) % TJ, ii = c / (TK * TJ);
+                const int i = b.i0 + tii * TI + ii, j = b.j0 + tj * TJ + jj, k = b.k0 + tk * TK + kk;
                 if (i >= b.i1 || j >= b.j1 || k >= b.k1) continue;
-                if (code == 0) flux_face<float, 0, false>(D.G, V, D.Vinit, D.sc, Fd, i, j, k);
-                else if (code == 1) flux_face<float, 1, false>(D.G, V, D.Vinit, D.sc, Fd, i, j, k);
-                else flux_face<float, 2, false>(D.G, V, D.Vinit, D.sc, Fd, i, j, k);
+                if (code == 0) flux_face<float, 0, false>(sG, V, D.Vinit, D.sc, Fd, i, j, k);
+                else if (code == 1) flux_face<float, 1, false>(sG, V, D.Vinit, D.sc, Fd, i, j, k);
+                else flux_face<float, 2, false>(sG, V, D.Vinit, D.sc, Fd, i, j, k);
             }
         } else if (live) {
             StageArgs<float> a;
             a.V = V; a.F = D.F; a.G = D.Gf; a.H = D.H; a.Un = D.U; a.U1 = D.U1;
             a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw;
-            a.sc = D.sc; a.trig = D.trig; a.kind = kind; a.last = last; a.counters = D.counters + 3 * stage;
+            a.sc = D.sc; a.trig = D.trig; a.trigf = D.trigf; a.kind = kind; a.last = last;
+            a.counters = D.counters + 3 * stage;
             int c0 = 0, c1 = 0, c2 = 0;
             if (code == 3) {
                 const Box &b = D.ubox;
                 const int ntk = D.ut[2], ntj = D.ut[1];
                 const int tk = local % ntk, tj = (local / ntk) % ntj, tii = local / (ntk * ntj);
-                const int n = cfg.ti * cfg.tj * cfg.tk;
+                constexpr int n = TI * TJ * TK;
                 for (int c = threadIdx.x; c < n; c += BT) {
-                    const int kk = c % cfg.tk, jj = (c / cfg.tk) % cfg.tj, ii = c / (cfg.tk * cfg.tj);
-                    const int i = b.i0 + tii * cfg.ti + ii, j = b.j0 + tj * cfg.tj + jj, k = b.k0 + tk * cfg.tk + kk;
+                    const int kk = c % TK, jj = (c / TK) % TJ, ii = c / (TK * TJ);
+                    const int i = b.i0 + tii * TI + ii, j = b.j0 + tj * TJ + jj, k = b.k0 + tk * TK + kk;
                     if (i >= b.i1 || j >= b.j1 || k >= b.k1) continue;
-                    int f = update_cell<float>(D.G, a, i, j, k);
+                    int f = update_cell<float>(sG, a, i, j, k);
                     c0 += f & 1; c1 += (f >> 1) & 1; c2 += (f >> 2) & 1;
                 }
             } else {
-                const unsigned ng = ghost_count(D.G);
+                const unsigned ng = ghost_count(sG);
                 const unsigned g0 = (unsigned)local * (unsigned)(4 * BT);
                 for (unsigned g = g0 + threadIdx.x; g < g0 + 4 * BT && g < ng; g += BT) {
-                    int f = ghost_cell<float>(D.G, a, g);
+                    int f = ghost_cell<float>(sG, a, g);
                     c0 += f & 1; c1 += (f >> 1) & 1; c2 += (f >> 2) & 1;
                 }
             }
@@ -271,6 +297,8 @@ __global__ void batch_trig_kernel(const DiscDev *__restrict__ discs)
         sincos(phase, &s, &c);
         D.trig[q] = c;
         D.trig[n + q] = s;
+        D.trigf[q] = (float)c;
+        D.trigf[n + q] = (float)s;
     }
 }
 
@@ -280,7 +308,78 @@ __global__ void batch_advance_kernel(const DiscDev *__restrict__ discs, int ndis
     if (d < ndisc && !discs[d].sc->dtbad) discs[d].sc->t += discs[d].sc->dt;
 }
 
-}  /* namespace */
+/* Phased mode: one specialised launch per phase over the tiles of every disc;
+ * stream order replaces the queue's waits.  A tile is 128 cells: by rows of
+ * j times bx cells along k, bx = the disc's k extent rounded up to a warp
+ * (at most 128). */
+__device__ __forceinline__ bool cell_of_tile(const uint4 e, const Box &b, int &i, int &j, int &k)
+{
+    const int bx = (int)(e.w >> 20), k0 = (int)(e.w & 0xfffffu);
+    i = (int)e.y;
+    j = (int)e.z + (int)threadIdx.x / bx;
+    k = k0 + (int)threadIdx.x % bx;
+    return (int)threadIdx.x < 128 / bx * bx && k < b.k1 && j < b.j1;
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(128) batch_flux_kernel(const DiscDev *__restrict__ discs,
+                                                         const uint4 *__restrict__ tiles, int parity)
+{
+    __shared__ Geom sG;
+    const uint4 e = tiles[blockIdx.x];
+    const DiscDev &D = discs[e.x];
+    load_geom(sG, D.G);
+    if (D.sc->dtbad) return;
+    int i, j, k;
+    if (!cell_of_tile(e, D.fbox[DIR], i, j, k)) return;
+    float *Fd = DIR == 0 ? D.F : DIR == 1 ? D.Gf : D.H;
+    flux_face<float, DIR, false>(sG, parity ? D.Vb : D.Va, D.Vinit, D.sc, Fd, i, j, k);
+}
+
+__device__ __forceinline__ StageArgs<float> stage_args(const DiscDev &D, int kind, int last, int parity, int stage)
+{
+    StageArgs<float> a;
+    a.V = parity ? D.Vb : D.Va; a.F = D.F; a.G = D.Gf; a.H = D.H; a.Un = D.U; a.U1 = D.U1;
+    a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw;
+    a.sc = D.sc; a.trig = D.trig; a.trigf = D.trigf; a.kind = kind; a.last = last;
+    a.counters = D.counters + 3 * stage;
+    return a;
+}
+
+__global__ void __launch_bounds__(128) batch_update_kernel(const DiscDev *__restrict__ discs,
+                                                           const uint4 *__restrict__ tiles, int kind, int last,
+                                                           int parity, int stage)
+{
+    __shared__ Geom sG;
+    const uint4 e = tiles[blockIdx.x];
+    const DiscDev &D = discs[e.x];
+    load_geom(sG, D.G);
+    if (D.sc->dtbad) return;
+    StageArgs<float> a = stage_args(D, kind, last, parity, stage);
+    int i, j, k, f = 0;
+    if (cell_of_tile(e, D.ubox, i, j, k)) f = update_cell<float>(sG, a, i, j, k);
+    add_counters(f, a.counters);
+}
+
+__global__ void __launch_bounds__(128) batch_ghost_kernel(const DiscDev *__restrict__ discs,
+                                                          const uint2 *__restrict__ tiles, int kind, int last,
+                                                          int parity, int stage)
+{
+    __shared__ Geom sG;
+    const uint2 e = tiles[blockIdx.x];
+    const DiscDev &D = discs[e.x];
+    load_geom(sG, D.G);
+    if (D.sc->dtbad) return;
+    StageArgs<float> a = stage_args(D, kind, last, parity, stage);
+    const unsigned g = e.y * blockDim.x + threadIdx.x;
+    int f = 0;
+    if (g < ghost_count(sG)) f = ghost_cell<float>(sG, a, g);
+    add_counters(f, a.counters);
+}
+
+}  /* namespace mhd_batch_k */
+
+using namespace mhd_batch_k;
 
 struct mhd_batch {
     int n, persistent, nst;
@@ -294,6 +393,11 @@ struct mhd_batch {
     /* tile tables */
     uint2 *dtiles, *ddt;
     int ntiles, ndt_tiles, rows_per_tile;
+    int phased;                 /* 1: one launch per phase, 0: one persistent launch per stage */
+    uint4 *dph[4];              /* phased row tiles: flux r, phi, z, update */
+    int nph[4];
+    uint2 *dghost;
+    int nghost_tiles;
     int *dqueue;    /* [3 stages]: head ; then done [3 stages][2*n] */
     int *derr;
     int *dcnt;      /* per disc [3][3] */
@@ -359,11 +463,12 @@ static int stage_blocks(TileCfg c)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     switch (c.variant) {
-    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<128, 4>, 128, 0); break;
-    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<128, 8>, 128, 0); break;
-    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<256, 2>, 256, 0); break;
-    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<256, 4>, 256, 0); break;
-    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<64, 8>, 64, 0); break;
+#define MHD_OCC(V, BT, MB, TI, TJ, TK)                                                                    \
+    case V: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<BT, MB, TI, TJ, TK>, BT, 0); \
+        break;
+        MHD_BATCH_VARIANTS(MHD_OCC)
+#undef MHD_OCC
+    default: break;
     }
     if (per < 1) per = 1;
     return sms * per;
@@ -371,19 +476,17 @@ static int stage_blocks(TileCfg c)
 
 static cudaError_t launch_stage(mhd_batch *b, int *head, int *done, int kind, int last, int parity, int stage)
 {
-    TileCfg c = b->cfg;
     int nb = b->nblk_stage;
-#define MHD_STAGE(BT, MB)                                                                                    \
-    batch_stage_kernel<BT, MB><<<nb, BT, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, done, b->n, b->derr, \
-                                                       kind, last, parity, stage, c)
-    switch (c.variant) {
-    case 0: MHD_STAGE(128, 4); break;
-    case 1: MHD_STAGE(128, 8); break;
-    case 2: MHD_STAGE(256, 2); break;
-    case 3: MHD_STAGE(256, 4); break;
-    default: MHD_STAGE(64, 8); break;
+    switch (b->cfg.variant) {
+#define MHD_LAUNCH(V, BT, MB, TI, TJ, TK)                                                                  \
+    case V:                                                                                                \
+        batch_stage_kernel<BT, MB, TI, TJ, TK><<<nb, BT, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, done, \
+                                                                     b->n, b->derr, kind, last, parity, stage); \
+        break;
+        MHD_BATCH_VARIANTS(MHD_LAUNCH)
+#undef MHD_LAUNCH
+    default: return cudaErrorInvalidValue;
     }
-#undef MHD_STAGE
     return cudaGetLastError();
 }
 
@@ -405,10 +508,20 @@ static int enqueue_batch_step(mhd_batch *b, int parity)
     int par = parity;
     for (int s = 0; s < b->nst; s++) {
         int kind = b->nst == 2 ? rk2[s][0] : rk3[s][0], last = b->nst == 2 ? rk2[s][1] : rk3[s][1];
-        int *q = b->dqueue + s * (1 + 2 * n);
-        BCK(cudaMemsetAsync(q, 0, (1 + 2 * n) * sizeof(int), b->st));
-        BCK(launch_stage(b, q, q + 1, kind, last, par, s));
-        b->launches++;
+        if (b->phased) {
+            batch_flux_kernel<0><<<b->nph[0], 128, 0, b->st>>>(b->dd, b->dph[0], par);
+            batch_flux_kernel<1><<<b->nph[1], 128, 0, b->st>>>(b->dd, b->dph[1], par);
+            batch_flux_kernel<2><<<b->nph[2], 128, 0, b->st>>>(b->dd, b->dph[2], par);
+            batch_update_kernel<<<b->nph[3], 128, 0, b->st>>>(b->dd, b->dph[3], kind, last, par, s);
+            batch_ghost_kernel<<<b->nghost_tiles, 128, 0, b->st>>>(b->dd, b->dghost, kind, last, par, s);
+            BCK(cudaGetLastError());
+            b->launches += 5;
+        } else {
+            int *q = b->dqueue + s * (1 + 2 * n);
+            BCK(cudaMemsetAsync(q, 0, (1 + 2 * n) * sizeof(int), b->st));
+            BCK(launch_stage(b, q, q + 1, kind, last, par, s));
+            b->launches++;
+        }
         par ^= 1;
     }
     batch_advance_kernel<<<ceil_div(n, 128), 128, 0, b->st>>>(b->dd, n);
@@ -452,7 +565,7 @@ static int setup_persistent(mhd_batch *b)
         D.U = (float *)c->U; D.U1 = (float *)c->U1; D.Va = (float *)c->Va; D.Vb = (float *)c->Vb;
         D.Uinit = (float *)c->Uinit; D.Vinit = (float *)c->Vinit; D.rhofloor = (float *)c->rhofloor;
         D.F = (float *)c->F; D.Gf = (float *)c->Gf; D.H = (float *)c->H; D.Uraw = (float *)c->Uraw;
-        D.sc = c->d_sc; D.trig = c->d_trig; D.part = c->d_part;
+        D.sc = c->d_sc; D.trig = c->d_trig; D.trigf = c->d_trigf; D.part = c->d_part;
         for (int dir = 0; dir < 3; dir++) {
             Box &bx = D.fbox[dir];
             bx.i0 = dir == 0 ? 0 : 1; bx.i1 = c->ixmax - 1;
@@ -500,6 +613,32 @@ static int setup_persistent(mhd_batch *b)
     int rc = build_tiles(b, CANDIDATES[0]);
     if (rc) return rc;
     b->nblk_stage = stage_blocks(b->cfg);
+    /* phased-mode tiles of 128 cells: by rows x bx cells along k */
+    for (int ph = 0; ph < 4; ph++) {
+        std::vector<uint4> tl;
+        for (int d = 0; d < n; d++) {
+            const Box &bx = ph < 3 ? b->hd[d].fbox[ph] : b->hd[d].ubox;
+            int nk = bx.k1 - bx.k0;
+            int wx = 32 * ceil_div(nk < 128 ? nk : 128, 32);
+            int by = 128 / wx;
+            for (int i = bx.i0; i < bx.i1; i++)
+                for (int j = bx.j0; j < bx.j1; j += by)
+                    for (int k0 = bx.k0; k0 < bx.k1; k0 += wx)
+                        tl.push_back(make_uint4(d, i, j, ((unsigned)wx << 20) | (unsigned)k0));
+        }
+        b->nph[ph] = (int)tl.size();
+        BCK(cudaMalloc((void **)&b->dph[ph], tl.size() * sizeof(uint4)));
+        BCK(cudaMemcpy(b->dph[ph], tl.data(), tl.size() * sizeof(uint4), cudaMemcpyHostToDevice));
+    }
+    std::vector<uint2> gt;
+    for (int d = 0; d < n; d++) {
+        const Geom &G = b->hd[d].G;
+        long long ng = 2LL * G.ixmax * G.jymax + 2LL * G.ixmax * (G.kzmax - 2) + 2LL * (G.jymax - 2) * (G.kzmax - 2);
+        for (long long l = 0; l * 128 < ng; l++) gt.push_back(make_uint2(d, (unsigned)l));
+    }
+    b->nghost_tiles = (int)gt.size();
+    BCK(cudaMalloc((void **)&b->dghost, gt.size() * sizeof(uint2)));
+    BCK(cudaMemcpy(b->dghost, gt.data(), gt.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     return MHD_OK;
 }
 
@@ -543,7 +682,8 @@ extern "C" void mhd_batch_destroy(mhd_batch *b)
     if (b->st) cudaStreamSynchronize(b->st);
     for (int q = 0; q < 2; q++)
         if (b->gx[q]) cudaGraphExecDestroy(b->gx[q]);
-    void *p[] = {b->dd, b->dtiles, b->ddt, b->dqueue, b->derr, b->dcnt};
+    void *p[] = {b->dd, b->dtiles, b->ddt, b->dqueue, b->derr, b->dcnt, b->dph[0], b->dph[1], b->dph[2],
+                 b->dph[3], b->dghost};
     for (size_t q = 0; q < sizeof p / sizeof p[0]; q++)
         if (p[q]) cudaFree(p[q]);
     if (b->st) cudaStreamDestroy(b->st);
@@ -590,7 +730,7 @@ static int batch_run(mhd_batch *b, int nsteps, double *t, int *status)
         int rc = build_graphs(b);
         if (rc) return rc;
     }
-    long long per_step = 3 + b->nst + 1;
+    long long per_step = 3 + b->nst * (b->phased ? 5 : 1) + 1;
     for (int s = 0; s < nsteps; s++) {
         BCK(cudaGraphLaunch(b->gx[b->parity], b->st));
         b->parity ^= (b->nst & 1);
@@ -633,7 +773,7 @@ extern "C" int mhd_batch_tune(mhd_batch *b, int *best)
 {
     if (!b || !best) return MHD_ERR_ARG;
     if (!b->persistent) {
-        best[0] = 1; best[1] = 1; best[2] = 128; best[3] = 128;
+        best[0] = 1; best[1] = 1; best[2] = 128; best[3] = 128; best[4] = 1;
         return MHD_OK;
     }
     const int n = b->n;
@@ -666,11 +806,14 @@ extern "C" int mhd_batch_tune(mhd_batch *b, int *best)
     BCK(cudaEventCreate(&e1));
     float best_ms = 1e30f;
     int best_i = 0;
-    for (int ci = 0; ci < NCAND; ci++) {
+    for (int ci = 0; ci <= NCAND; ci++) {   /* NCAND = the phased mode */
         int rc = restore();
         if (rc) return rc;
-        if ((rc = build_tiles(b, CANDIDATES[ci]))) return rc;
-        b->nblk_stage = stage_blocks(b->cfg);
+        b->phased = ci == NCAND;
+        if (!b->phased) {
+            if ((rc = build_tiles(b, CANDIDATES[ci]))) return rc;
+            b->nblk_stage = stage_blocks(b->cfg);
+        }
         b->graph_ready = 0;
         tt = t0;
         if ((rc = batch_run(b, 1, tt.data(), NULL))) return rc;   /* warm-up + graph build */
@@ -687,13 +830,21 @@ extern "C" int mhd_batch_tune(mhd_batch *b, int *best)
     int rc = restore();
     if (rc) return rc;
     for (int d = 0; d < n; d++) b->ctx[d]->h_sc->t = t0[d];
-    if ((rc = build_tiles(b, CANDIDATES[best_i]))) return rc;
-    b->nblk_stage = stage_blocks(b->cfg);
+    b->phased = best_i == NCAND;
+    if (!b->phased) {
+        if ((rc = build_tiles(b, CANDIDATES[best_i]))) return rc;
+        b->nblk_stage = stage_blocks(b->cfg);
+    }
     b->graph_ready = 0;
     (void)par0;
-    best[0] = CANDIDATES[best_i].ti;
-    best[1] = CANDIDATES[best_i].tj;
-    best[2] = CANDIDATES[best_i].tk;
-    best[3] = CANDIDATES[best_i].bt;
+    if (b->phased) {
+        best[0] = 1; best[1] = 1; best[2] = 128; best[3] = 128; best[4] = 1;
+    } else {
+        best[0] = CANDIDATES[best_i].ti;
+        best[1] = CANDIDATES[best_i].tj;
+        best[2] = CANDIDATES[best_i].tk;
+        best[3] = CANDIDATES[best_i].bt;
+        best[4] = 0;
+    }
     return MHD_OK;
 }

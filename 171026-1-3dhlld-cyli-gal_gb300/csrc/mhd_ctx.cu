@@ -97,7 +97,8 @@ static void *vnext_ptr(mhd_ctx *ctx) { return ctx->vcur == 0 ? ctx->Vb : ctx->Va
  * for the precision form; the plain form fills the same table on the host
  * with the C library's sincos, the function the reference calls. */
 __global__ void trig_kernel(int ixmax, int jymax, const double *__restrict__ y, const double *__restrict__ spL,
-                            double armnum, double omdiff, const StepScalars *__restrict__ sc, double *trig)
+                            double armnum, double omdiff, const StepScalars *__restrict__ sc, double *trig,
+                            float *trigf)
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)ixmax * jymax) return;
@@ -107,6 +108,8 @@ __global__ void trig_kernel(int ixmax, int jymax, const double *__restrict__ y, 
     sincos(phase, &s, &c);
     trig[t] = c;
     trig[(long long)ixmax * jymax + t] = s;
+    trigf[t] = (float)c;
+    trigf[(long long)ixmax * jymax + t] = (float)s;
 }
 
 __global__ void gravity_probe_kernel(Geom G, const StepScalars *__restrict__ sc, const double *__restrict__ trig,
@@ -158,7 +161,7 @@ static int gather_ik(const double *src, int compact, int ni, int nj, int nk, int
 static void free_all(mhd_ctx *ctx)
 {
     void *dev[] = {ctx->dtab, ctx->ftab, ctx->U, ctx->U1, ctx->Va, ctx->Vb, ctx->Uinit, ctx->Vinit,
-                   ctx->rhofloor, ctx->F, ctx->Gf, ctx->H, ctx->Uraw, ctx->d_sc, ctx->d_trig,
+                   ctx->rhofloor, ctx->F, ctx->Gf, ctx->H, ctx->Uraw, ctx->d_sc, ctx->d_trig, ctx->d_trigf,
                    ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run};
     for (size_t q = 0; q < sizeof dev / sizeof dev[0]; q++)
         if (dev[q]) cudaFree(dev[q]);
@@ -310,6 +313,9 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     G.spA = D + o_spA; G.spS = D + o_spS; G.spQ = D + o_spQ; G.spR = D + o_spR;
     G.spC1 = D + o_C1; G.spC2 = D + o_C2; G.spD = D + o_D; G.spL = D + o_L; G.y = D + o_y; G.z = D + o_z;
     G.dvol = D + o_dvol; G.dy = g->dy;
+    G.graxif = Fd + o_grax; G.spAf = Fd + o_spA; G.spSf = Fd + o_spS; G.spQf = Fd + o_spQ; G.spRf = Fd + o_spR;
+    G.spC1f = Fd + o_C1; G.spC2f = Fd + o_C2; G.spDf = Fd + o_D; G.zf = Fd + o_z;
+    G.armnumf = (float)p->armnum; G.cotpitchf = (float)cotpitch;
     G.omegasp = p->omegasp; G.prcr = p->prcr; G.betacr = p->betacr; G.rhocr = p->rhocr;
     G.armnum = (double)p->armnum; G.cotpitch = cotpitch;
     G.cooling = p->cooling; G.gravity = p->gravity; G.limiter = p->limiter; G.solver = p->solver;
@@ -332,6 +338,8 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     size_t ntrig = 2 * (size_t)ixmax * jymax;
     CKC(cudaMalloc((void **)&ctx->d_trig, ntrig * sizeof(double)));
     CKC(cudaMemset(ctx->d_trig, 0, ntrig * sizeof(double)));
+    CKC(cudaMalloc((void **)&ctx->d_trigf, ntrig * sizeof(float)));
+    CKC(cudaMemset(ctx->d_trigf, 0, ntrig * sizeof(float)));
     CKC(cudaMallocHost((void **)&ctx->h_trig, ntrig * sizeof(double)));
     long long ndt = (long long)(ixmax - 12) * (jymax - 2) * (kzmax - 2);
     ctx->npart = (int)((ndt + 255) / 256);
@@ -507,7 +515,7 @@ extern "C" int mhd_spiral_gravity(mhd_ctx *ctx, double t)
         CK(prof_begin(ctx, PK_TRIG));
         trig_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->st>>>(ixmax, jymax, ctx->G.y, ctx->G.spL,
                                                                        (double)p->armnum, ctx->omdiff, ctx->d_sc,
-                                                                       ctx->d_trig);
+                                                                       ctx->d_trig, ctx->d_trigf);
         CK(cudaGetLastError());
         CK(prof_end(ctx));
     }
@@ -540,7 +548,7 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     a.Un = (T *)ctx->U; a.U1 = (T *)ctx->U1;
     a.Uinit = (const T *)ctx->Uinit; a.rhofloor = (const T *)ctx->rhofloor;
     a.Vout = (T *)vnext_ptr(ctx); a.Uraw = (T *)ctx->Uraw;
-    a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.kind = kind; a.last = last; a.counters = counters;
+    a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.trigf = ctx->d_trigf; a.kind = kind; a.last = last; a.counters = counters;
     LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
     LAUNCH(PK_GHOST, launch_ghost(ctx->G, a, ctx->st));
     ctx->vcur ^= 1;
@@ -662,10 +670,10 @@ extern "C" int mhd_dbg_source(mhd_ctx *ctx, double *S)
     double *d_S = NULL;
     CK(cudaMemcpyAsync(ctx->d_sc, ctx->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMallocAsync((void **)&d_S, 9 * ctx->nc * sizeof(double), ctx->st));
-    cudaError_t e = ctx->fp32 ? launch_source(ctx->G, (const float *)vcur_ptr(ctx), ctx->d_sc, ctx->d_trig, d_S,
-                                              ctx->st)
+    cudaError_t e = ctx->fp32 ? launch_source(ctx->G, (const float *)vcur_ptr(ctx), ctx->d_sc, ctx->d_trig,
+                                              ctx->d_trigf, d_S, ctx->st)
                               : launch_source(ctx->G, (const double *)vcur_ptr(ctx), ctx->d_sc, ctx->d_trig,
-                                              d_S, ctx->st);
+                                              ctx->d_trigf, d_S, ctx->st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(S, d_S, 9 * ctx->nc * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
     cudaFreeAsync(d_S, ctx->st);
@@ -757,7 +765,8 @@ static int enqueue_device_step(mhd_ctx *ctx)
         long long n = (long long)ctx->ixmax * ctx->jymax;
         trig_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->st>>>(ctx->ixmax, ctx->jymax, ctx->G.y,
                                                                        ctx->G.spL, (double)p->armnum,
-                                                                       ctx->omdiff, ctx->d_sc, ctx->d_trig);
+                                                                       ctx->omdiff, ctx->d_sc, ctx->d_trig,
+                                                                       ctx->d_trigf);
         CK(cudaGetLastError());
         ctx->launches++;
     }

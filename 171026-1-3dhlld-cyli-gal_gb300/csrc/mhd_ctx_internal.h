@@ -26,6 +26,7 @@ struct mhd_ctx {
     int vcur;
     mhd::StepScalars *d_sc, *h_sc;
     double *d_trig, *h_trig;
+    float *d_trigf;
     mhd::MaxLoc *d_part, *h_part;
     int npart;
     int *d_cnt, *h_cnt;

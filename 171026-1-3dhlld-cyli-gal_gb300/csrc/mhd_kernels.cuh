@@ -134,7 +134,7 @@ __device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a,
     T W[9], S[9], u[9];
 #pragma unroll
     for (int m = 0; m < 9; m++) W[m] = V[m * nc + q];
-    source_at<T>(G, *sc, a.trig, i, j, k, W, S);
+    source_at<T>(G, *sc, a.trig, a.trigf, i, j, k, W, S);
 #pragma unroll
     for (int m = 0; m < 9; m++) {
         const long long mq = m * nc + q;
@@ -369,7 +369,8 @@ __global__ void cvt_to_f64(const T *__restrict__ src, double *__restrict__ dst, 
 /* source term probe (SpiralGravityCooling over all cells) */
 template <typename T>
 __global__ void source_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc,
-                              const double *__restrict__ trig, double *__restrict__ S)
+                              const double *__restrict__ trig, const float *__restrict__ trigf,
+                              double *__restrict__ S)
 {
     long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= G.nc) return;
@@ -380,7 +381,7 @@ __global__ void source_kernel(Geom G, const T *__restrict__ V, const StepScalars
     T W[9], Sv[9];
 #pragma unroll
     for (int m = 0; m < 9; m++) W[m] = V[m * G.nc + tid];
-    source_at<T>(G, *sc, trig, i, j, k, W, Sv);
+    source_at<T>(G, *sc, trig, trigf, i, j, k, W, Sv);
 #pragma unroll
     for (int m = 0; m < 9; m++) S[m * G.nc + tid] = (double)Sv[m];
 }
@@ -456,10 +457,10 @@ cudaError_t launch_setdt_t(const Geom &G, const T *V, MaxLoc *part, int nblk, cu
 }
 
 template <typename T>
-cudaError_t launch_source_t(const Geom &G, const T *V, const StepScalars *sc, const double *trig, double *S,
-                            cudaStream_t st)
+cudaError_t launch_source_t(const Geom &G, const T *V, const StepScalars *sc, const double *trig,
+                            const float *trigf, double *S, cudaStream_t st)
 {
-    source_kernel<T><<<nblocks(G.nc, 128), 128, 0, st>>>(G, V, sc, trig, S);
+    source_kernel<T><<<nblocks(G.nc, 128), 128, 0, st>>>(G, V, sc, trig, trigf, S);
     return cudaGetLastError();
 }
 
@@ -505,9 +506,9 @@ cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream
         return launch_setdt_t<T>(G, V, part, nblk, st);                                                      \
     }                                                                                                        \
     cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
-                              double *S, cudaStream_t st)                                                    \
+                              const float *trigf, double *S, cudaStream_t st)                                \
     {                                                                                                        \
-        return launch_source_t<T>(G, V, sc, trig, S, st);                                                    \
+        return launch_source_t<T>(G, V, sc, trig, trigf, S, st);                                             \
     }                                                                                                        \
     cudaError_t launch_cvt(const double *src, T *dst, long long n, cudaStream_t st)                          \
     {                                                                                                        \

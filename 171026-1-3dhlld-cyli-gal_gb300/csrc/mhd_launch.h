@@ -29,6 +29,7 @@ struct StageArgs {
     T *Vout, *Uraw;
     const StepScalars *sc;
     const double *trig;
+    const float *trigf;
     int kind, last;
     int *counters;
 };
@@ -42,7 +43,7 @@ struct StageArgs {
     cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                         \
     cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st);            \
     cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
-                              double *S, cudaStream_t st);                                                   \
+                              const float *trigf, double *S, cudaStream_t st);                               \
     cudaError_t launch_cvt(const double *src, T *dst, long long n, cudaStream_t st);                         \
     cudaError_t launch_cvt_back(const T *src, double *dst, long long n, cudaStream_t st);
 

@@ -438,7 +438,7 @@ class Batch:
         return t, st
 
     def tune(self):
-        best = np.zeros(4, dtype=np.int32)
+        best = np.zeros(5, dtype=np.int32)
         check(lib().mhd_batch_tune(self.h, best), "mhd_batch_tune")
         return tuple(int(v) for v in best)
 

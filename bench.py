@@ -233,6 +233,90 @@ def precision_report(args):
     return 0
 
 
+def batch_bench(args):
+    """Batched workload: 64 uneven discs (sizes from seed 7), precision form.
+    value = all zones of all discs x steps / device time of the persistent
+    batched step (after mhd_batch_tune); sequential = the same discs stepped
+    one after another with the single-disc device-resident path (mhd_run).
+    --batch-check N adds each disc's error against its own plain FP64 run
+    after N steps."""
+    M = load_product()
+    n = int(args.workload[5:] or 64)
+    wl = M.batch_workload(n=n, seed=7)
+    grids, params, states = [], [], []
+    for dims, p, ic in wl:
+        g = M.Grid.disc(*dims)
+        g.set_initial_gravity()
+        U, V = g.ic_disc(**ic)
+        grids.append(g)
+        params.append(p)
+        states.append((U, V))
+    zones = sum(g.ix * g.jy * g.kz for g in grids)
+    b = M.Batch(grids, params)
+    for d, (U, V) in enumerate(states):
+        b.upload(d, U, V)
+    t = np.zeros(n)
+    t, st = b.step(1, t)
+    w0 = time.perf_counter()
+    best = b.tune()
+    tune_s = time.perf_counter() - w0
+    t, st = b.step(args.warmup, t)
+    sampler = ClockSampler()
+    sampler.start()
+    time.sleep(0.3)
+    w0 = time.perf_counter()
+    t, st = b.step(args.steps, t)
+    wall = time.perf_counter() - w0
+    clocks = sampler.stop()
+    stopped = int((st != 0).sum())
+    b.close()
+    # sequential single-disc device-resident path
+    seq_wall = 0.0
+    for d in range(n):
+        disc = M.Disc(grids[d], params[d])
+        disc.upload(*states[d])
+        tt = disc.run(1 + args.warmup, 0.0)
+        w0 = time.perf_counter()
+        disc.run(args.steps, tt)
+        seq_wall += time.perf_counter() - w0
+        disc.close()
+    out = {"metric": "zone-updates/s, batched discs (FP32 + FP64 repair)", "workload": "batch%d" % n,
+           "discs": n, "zones": zones, "steps": args.steps, "warmup": args.warmup,
+           "value": zones * args.steps / wall, "unit": "zone-updates/s", "ms_per_step": wall / args.steps * 1e3,
+           "sequential_single_disc": {"value": zones * args.steps / seq_wall, "ms_per_step": seq_wall / args.steps * 1e3},
+           "tuned": {"tile_r": best[0], "tile_phi": best[1], "tile_z": best[2], "threads": best[3],
+                     "mode": "phased" if best[4] else "persistent", "tune_seconds": tune_s},
+           "discs_stopped_by_dt_guard": stopped, "clocks": clocks,
+           "sizes": [list(dims) for dims, _, _ in wl]}
+    if args.batch_check:
+        errs = []
+        b = M.Batch(grids, params)
+        for d, (U, V) in enumerate(states):
+            b.upload(d, U, V)
+        b.step(args.batch_check, np.zeros(n))
+        for d in range(n):
+            pd = params[d].as_dict()
+            pd.pop("precision")
+            s64 = M.Disc(grids[d], M.default_params(precision="fp64", **pd))
+            s64.upload(*states[d])
+            tt = 0.0
+            for _ in range(args.batch_check):
+                rc, tt, *_ = s64.step(tt)
+            U64, _ = s64.download()
+            s64.close()
+            Ub, _ = b.download(d)
+            rl = [float(np.abs(Ub[m] - U64[m]).sum() / max(np.abs(U64[m]).sum(), 1e-300)) for m in range(9)]
+            errs.append(rl)
+        b.close()
+        errs = np.array(errs)
+        names = ["rho", "m_r", "r*m_phi", "m_z", "B_r", "B_phi", "B_z", "E", "psi"]
+        out["fp64_check"] = {"steps": args.batch_check,
+                             "max_over_discs_rel_l1": dict(zip(names, errs.max(axis=0).tolist())),
+                             "median_over_discs_rel_l1": dict(zip(names, np.median(errs, axis=0).tolist()))}
+    print(json.dumps(out))
+    return 0
+
+
 def rank_info():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -260,9 +344,12 @@ def main():
     ap.add_argument("--precision-report", type=int, default=0, metavar="NSTEPS",
                     help="run both forms NSTEPS steps and report the FP32 form's error")
     ap.add_argument("--solver", default=None, help="hlld or hll")
+    ap.add_argument("--batch-check", type=int, default=0, metavar="NSTEPS")
     args = ap.parse_args()
     if args.precision_report:
         return precision_report(args)
+    if args.workload.startswith("batch"):
+        return batch_bench(args)
     rank, world, local = rank_info()
     dims = tuple(int(v) for v in args.size.split("x")) if args.size else (512, 512, 256)
     zones = dims[0] * dims[1] * dims[2]

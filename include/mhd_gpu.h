@@ -213,8 +213,11 @@ int mhd_batch_download(mhd_batch *b, int disc, double *U, double *V);
  * stops advancing).  One persistent launch per RK stage, the whole step
  * captured as a CUDA graph. */
 int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status);
-/* Times candidate tile shapes on the current state and keeps the fastest;
- * the state is restored afterwards.  best[4] = {tile_i, tile_j, tile_k, threads}. */
+/* Times candidate configurations on the current state and keeps the fastest;
+ * the state is restored afterwards.  Candidates: the persistent per-stage
+ * launch with each compiled tile shape / block size / register cap, and the
+ * phased form (one launch per stage phase over all discs).
+ * best[5] = {tile_i, tile_j, tile_k, threads, phased}. */
 int mhd_batch_tune(mhd_batch *b, int *best);
 
 /* ---- allocation-free CFL reduction -------------------------------------- */
