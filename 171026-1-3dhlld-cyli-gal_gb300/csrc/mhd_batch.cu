@@ -167,7 +167,7 @@ batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ 
         } else if (live) {
             StageArgs<float> a;
             a.V = V; a.F = D.F; a.G = D.Gf; a.H = D.H; a.Un = D.U; a.U1 = D.U1;
-            a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw;
+            a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw; a.Vinit = D.Vinit;
             a.sc = D.sc; a.trig = D.trig; a.trigf = D.trigf; a.kind = kind; a.last = last;
             a.counters = D.counters + 3 * stage;
             int c0 = 0, c1 = 0, c2 = 0;
@@ -340,7 +340,7 @@ __device__ __forceinline__ StageArgs<float> stage_args(const DiscDev &D, int kin
 {
     StageArgs<float> a;
     a.V = parity ? D.Vb : D.Va; a.F = D.F; a.G = D.Gf; a.H = D.H; a.Un = D.U; a.U1 = D.U1;
-    a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw;
+    a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw; a.Vinit = D.Vinit;
     a.sc = D.sc; a.trig = D.trig; a.trigf = D.trigf; a.kind = kind; a.last = last;
     a.counters = D.counters + 3 * stage;
     return a;

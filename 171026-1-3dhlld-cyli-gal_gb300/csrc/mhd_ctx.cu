@@ -29,7 +29,7 @@ using namespace mhd;
 
 
 enum { PK_FLUX_R = 0, PK_FLUX_PHI = 1, PK_FLUX_Z = 2, PK_UPDATE = 3, PK_GHOST = 4, PK_SETDT = 5, PK_TRIG = 6,
-       PK_CVT = 7 };
+       PK_CVT = 7, PK_STAGE = 8 };
 static const int MAXSLOT = 256;
 
 /* fold the recorded event pairs into the per-kind totals */
@@ -197,6 +197,9 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
 
     ctx = new (std::nothrow) mhd_ctx();
     if (!ctx) return MHD_ERR_NOMEM;
+    ctx->fused = 0;
+    ctx->stage_tj = 7;
+    ctx->stage_seg = 32;
     memset((void *)&ctx->G, 0, sizeof ctx->G);
     cudaGetDevice(&ctx->device);
     ctx->p = *p;
@@ -294,6 +297,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     } while (0)
 
     CKC(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+    CKC(ctx->fp32 ? prepare_stage((float *)0) : prepare_stage((double *)0));
     CKC(cudaMalloc((void **)&ctx->dtab, T.size() * sizeof(double)));
     CKC(cudaMalloc((void **)&ctx->ftab, TF.size() * sizeof(float)));
     CKC(cudaMemcpy(ctx->dtab, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -540,16 +544,21 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     const T *V = (const T *)vcur_ptr(ctx);
     const T *Vinit = (const T *)ctx->Vinit;
     T *F = (T *)ctx->F, *Gf = (T *)ctx->Gf, *H = (T *)ctx->H;
-    LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
-    LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
-    LAUNCH(PK_FLUX_Z, launch_flux(2, ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), false, ctx->st));
     StageArgs<T> a;
     a.V = V; a.F = F; a.G = Gf; a.H = H;
     a.Un = (T *)ctx->U; a.U1 = (T *)ctx->U1;
     a.Uinit = (const T *)ctx->Uinit; a.rhofloor = (const T *)ctx->rhofloor;
     a.Vout = (T *)vnext_ptr(ctx); a.Uraw = (T *)ctx->Uraw;
     a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.trigf = ctx->d_trigf; a.kind = kind; a.last = last; a.counters = counters;
-    LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
+    a.Vinit = Vinit;
+    if (ctx->fused) {
+        LAUNCH(PK_STAGE, launch_stage(ctx->G, a, ctx->stage_tj, ctx->stage_seg, ctx->st));
+    } else {
+        LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
+        LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
+        LAUNCH(PK_FLUX_Z, launch_flux(2, ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), false, ctx->st));
+        LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
+    }
     LAUNCH(PK_GHOST, launch_ghost(ctx->G, a, ctx->st));
     ctx->vcur ^= 1;
     return MHD_OK;
@@ -909,6 +918,22 @@ extern "C" int mhd_prof_enable(mhd_ctx *ctx, int on)
     ctx->nslot = 0;
     for (int k = 0; k < MHD_PROF_NKIND; k++) { ctx->prof_ms[k] = 0.0; ctx->prof_n[k] = 0; }
     ctx->prof = on ? 1 : 0;
+    return MHD_OK;
+}
+
+extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
+{
+    if (!ctx || (fused != 0 && fused != 1) || tj != 7 || seg < 1) return MHD_ERR_ARG;
+    ctx->fused = fused;
+    ctx->stage_tj = tj;
+    ctx->stage_seg = seg;
+    if (ctx->graph_ready) {
+        /* the captured step graphs bake in the old shape */
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int q = 0; q < 2; q++)
+            if (ctx->gexecs[q]) { cudaGraphExecDestroy(ctx->gexecs[q]); ctx->gexecs[q] = NULL; }
+        ctx->graph_ready = 0;
+    }
     return MHD_OK;
 }
 

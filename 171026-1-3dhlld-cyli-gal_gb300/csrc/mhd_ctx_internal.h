@@ -24,6 +24,9 @@ struct mhd_ctx {
     float *ftab;
     void *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
     int vcur;
+    /* stage shape: fused = one kernel for fluxes + update (else the four
+     * separate kernels), tile height tj (j) and run length seg (i) */
+    int fused, stage_tj, stage_seg;
     mhd::StepScalars *d_sc, *h_sc;
     double *d_trig, *h_trig;
     float *d_trigf;

@@ -3,7 +3,8 @@
  * instantiated once per precision form by mhd_fp64.cu / mhd_fp32.cu (which
  * differ only in compile flags).
  *
- * One RK stage = flux(r) + flux(phi) + flux(z) + update + ghost:
+ * One RK stage = flux(r) + flux(phi) + flux(z) + update + ghost, or the fused
+ * stage kernel (all four in one launch) + ghost:
  *   flux    one thread per face the update reads; reconstruction of the two
  *           adjacent cells, Riemann solver, GLM flux -> F/G/H[9][cells]
  *   update  one thread per interior cell: sources, the stage's conservative
@@ -60,6 +61,26 @@ flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const 
     flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, i, j, k);
 }
 
+/* The two z boundary faces of each (i,j) column (face 0 and face kzmax-2,
+ * which take the special left/right states of face_states), one thread per
+ * face with the side slowest so every warp takes one branch; the interior
+ * z faces run in flux_kernel<T,2> without that divergence. */
+template <typename T, bool REFLAYOUT>
+__global__ void __launch_bounds__(128)
+flux_zedge_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
+                  T *__restrict__ F, Box b, int lo, int hi)
+{
+    const int nj = b.j1 - b.j0;
+    const long long nij = (long long)(b.i1 - b.i0) * nj;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nij * (lo + hi)) return;
+    const int s = (int)(t / nij);
+    const long long r = t - s * nij;
+    const int k = (lo && s == 0) ? 0 : G.kzmax - 2;
+    const int i = b.i0 + (int)(r / nj), j = b.j0 + (int)(r % nj);
+    flux_face<T, 2, REFLAYOUT>(G, V, Vinit, sc, F, i, j, k);
+}
+
 /* reconstructed face states in the reference's face layout (probe) */
 template <typename T, int DIR>
 __global__ void __launch_bounds__(128)
@@ -113,23 +134,36 @@ __device__ __forceinline__ void absorb(const Geom &G, const T *__restrict__ Uini
     }
 }
 
-/* kind: 0 U1=U-dtL (Halfstep/FirstStep), 1 U1=(3U+U1-dtL)/4 (SecondStep),
- *       2 U=(U+2(U1-dtL))/3 (ThirdStep), 3 U=(U+U1-dtL)/2 (Fullstep) */
+/* the six geometric factors of cell (i,k) (cylindricalgrid.h:120-125):
+ * g[0..5] = g1..g6, weights of the lower/upper r, phi and z face fluxes */
 template <typename T>
-__device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a, int i, int j, int k)
+__device__ __forceinline__ void geo_factors(const Geom &G, int i, int k, T g[6])
 {
     const Tabs<T> &tb = tabs<T>(G);
+    const long long gk = (long long)i * G.kzmax + k, pl = (long long)G.ixmax * G.kzmax;
+#pragma unroll
+    for (int s = 0; s < 6; s++) g[s] = tb.g[s * pl + gk];
+}
+
+/* flux divergence of one variable from its six face fluxes, in the
+ * reference's order (firststep.h:105-110) */
+template <typename T>
+__device__ __forceinline__ T flux_div(const T g[6], T fu, T fl, T gu, T gl, T hu, T hl)
+{
+    return ((g[1] * fu - g[0] * fl) + (g[3] * gu - g[2] * gl) + (g[5] * hu - g[4] * hl));
+}
+
+/* kind: 0 U1=U-dtL (Halfstep/FirstStep), 1 U1=(3U+U1-dtL)/4 (SecondStep),
+ *       2 U=(U+2(U1-dtL))/3 (ThirdStep), 3 U=(U+U1-dtL)/2 (Fullstep)
+ * div[] = the flux divergence of each variable at (i,j,k). */
+template <typename T>
+__device__ __forceinline__ int update_apply(const Geom &G, const StageArgs<T> &a, int i, int j, int k,
+                                            const T div[9])
+{
     const StepScalars *sc = a.sc;
     const long long nc = G.nc, q = cidx(G, i, j, k);
-    const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
-    const long long gk = (long long)i * G.kzmax + k, pl = (long long)G.ixmax * G.kzmax;
-    const T g1 = tb.g[gk], g2 = tb.g[pl + gk], g3 = tb.g[2 * pl + gk];
-    const T g4 = tb.g[3 * pl + gk], g5 = tb.g[4 * pl + gk], g6 = tb.g[5 * pl + gk];
     const T dt = Scal<T>::dt(sc), psicoef = Scal<T>::psi(sc);
     const T *__restrict__ V = a.V;
-    const T *__restrict__ F = a.F;
-    const T *__restrict__ Gf = a.G;
-    const T *__restrict__ H = a.H;
     const int kind = a.kind;
     T W[9], S[9], u[9];
 #pragma unroll
@@ -138,14 +172,13 @@ __device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a,
 #pragma unroll
     for (int m = 0; m < 9; m++) {
         const long long mq = m * nc + q;
-        T div = ((g2 * F[mq] - g1 * F[mq - si]) + (g4 * Gf[mq] - g3 * Gf[mq - sj]) + (g6 * H[mq] - g5 * H[mq - 1]));
         T un = a.Un[mq], u1 = (kind == 0) ? T(0) : a.U1[mq];
         if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
         T v;
-        if (kind == 0) v = un - dt * div + dt * S[m];
-        else if (kind == 1) v = T(0.25) * (T(3.0) * un + u1 - dt * div + dt * S[m]);
-        else if (kind == 2) v = T(MHD_ONEO3) * (un + T(2.0) * (u1 - dt * div + dt * S[m]));
-        else v = T(0.5) * (un + u1 - dt * div + dt * S[m]);
+        if (kind == 0) v = un - dt * div[m] + dt * S[m];
+        else if (kind == 1) v = T(0.25) * (T(3.0) * un + u1 - dt * div[m] + dt * S[m]);
+        else if (kind == 2) v = T(MHD_ONEO3) * (un + T(2.0) * (u1 - dt * div[m] + dt * S[m]));
+        else v = T(0.5) * (un + u1 - dt * div[m] + dt * S[m]);
         u[m] = v;
     }
     if (is_bc_source(G, i, j, k)) {
@@ -161,8 +194,22 @@ __device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a,
     return flags;
 }
 
-/* kind: 0 U1=U-dtL (Halfstep/FirstStep), 1 U1=(3U+U1-dtL)/4 (SecondStep),
- *       2 U=(U+2(U1-dtL))/3 (ThirdStep), 3 U=(U+U1-dtL)/2 (Fullstep) */
+/* update of one interior cell from the face fluxes in F/G/H */
+template <typename T>
+__device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a, int i, int j, int k)
+{
+    const long long nc = G.nc, q = cidx(G, i, j, k);
+    const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
+    T g[6], div[9];
+    geo_factors<T>(G, i, k, g);
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+        const long long mq = m * nc + q;
+        div[m] = flux_div<T>(g, a.F[mq], a.F[mq - si], a.G[mq], a.G[mq - sj], a.H[mq], a.H[mq - 1]);
+    }
+    return update_apply<T>(G, a, i, j, k, div);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) update_kernel(Geom G, StageArgs<T> a)
 {
@@ -173,6 +220,147 @@ __global__ void __launch_bounds__(128) update_kernel(Geom G, StageArgs<T> a)
     int flags = 0;
     if (k < G.kzmax - 1 && j < G.jymax - 1) flags = update_cell<T>(G, a, i, j, k);
     add_counters(flags, a.counters);
+}
+
+/* ------------------------------------------------------------------------ */
+/* fused stage: fluxes and update of the interior in one kernel              */
+/* ------------------------------------------------------------------------ */
+/* Riemann + GLM flux of face (i,j,k) along DIR (face index convention of
+ * flux_face: face f lies between cells f and f+1) into Fo */
+template <typename T, int DIR>
+__device__ __forceinline__ void face_flux_at(const Geom &G, const T *__restrict__ V, const T *__restrict__ Vinit,
+                                             const StepScalars *__restrict__ sc, int i, int j, int k, T Fo[9])
+{
+    T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
+    T L[9], R[9];
+    face_states<T, DIR>(G, V, Vinit, i, j, k, dt, psicoef, L, R);
+    face_flux<T, DIR>(G, L, R, i, ch, Fo);
+}
+
+/* L2 prefetch of the bytes of elements [e0, e1) of array p (n elements) through
+ * the bulk-copy unit: one instruction per contiguous run.  The range is clipped
+ * to the array and to 16-byte boundaries inside it (the array base is
+ * 256-byte aligned), so no byte outside the allocation is named. */
+template <typename T>
+__device__ __forceinline__ void prefetch_run(const T *p, long long n, long long e0, long long e1)
+{
+    if (e0 < 0) e0 = 0;
+    if (e1 > n) e1 = n;
+    if (e1 <= e0) return;
+    unsigned long long s = (unsigned long long)(p + e0) & ~15ull;
+    unsigned long long e = (unsigned long long)(p + e1) & ~15ull;
+    if (e > s)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s), "r"((unsigned)(e - s)) : "memory");
+}
+
+/* One block = a tile of 32 (k) x TJ (j) cells marching over a run of seg
+ * planes in i, with TJ + 1 warps: warp w >= 1 owns row j0 + w - 1, warp 0
+ * is the tile's helper.  Per plane each row warp forms the r, phi and z
+ * fluxes of its cells' upper faces (three face rounds); the helper forms the
+ * tile's lower phi faces (one round) and lower z faces (one partial round)
+ * and issues the L2 prefetches of the next plane's inputs, so every warp's
+ * path to the barrier is at most three rounds.  The r flux of a cell's lower
+ * face is the previous plane's upper one.  The face fluxes meet in shared
+ * memory (double-buffered by plane, so one barrier per plane suffices) and
+ * never travel to HBM; every face of the stage is computed once, plus one r
+ * face per run and the tile's edge faces.  The update, sources, UtoV and
+ * Check follow in the same thread: one launch replaces the flux(r),
+ * flux(phi), flux(z) and update kernels. */
+template <typename T, int TJ>
+struct StageSmem {
+    T fr[2][TJ][9][32];        /* r fluxes of the lower / upper face, ping-pong by plane */
+    T fg[2][TJ + 1][9][32];    /* phi faces: [plane parity][s] = face j0 + s - 1 */
+    T fh[2][TJ][9][33];        /* z faces: [plane parity][row][s] = face k0 + s - 1 */
+};
+
+template <typename T, int TJ, int MINB>
+__global__ void __launch_bounds__(32 * (TJ + 1), MINB) stage_kernel(Geom G, StageArgs<T> a, int seg)
+{
+    if (a.sc->dtbad) return;
+    extern __shared__ __align__(16) unsigned char stage_smem_raw[];
+    StageSmem<T, TJ> &sm = *reinterpret_cast<StageSmem<T, TJ> *>(stage_smem_raw);
+    const int lane = threadIdx.x, w = threadIdx.y, jj = w - 1;
+    const int k0 = 1 + blockIdx.x * 32, j0 = 1 + blockIdx.y * TJ;
+    const int k = k0 + lane, j = j0 + jj;
+    const int ia = 1 + blockIdx.z * seg;
+    const int ib = min(ia + seg, G.ixmax - 1);
+    const bool kin = k < G.kzmax - 1;
+    const bool live = w > 0 && kin && j < G.jymax - 1;
+    const T *__restrict__ V = a.V;
+    const T *__restrict__ Vinit = a.Vinit;
+    const StepScalars *__restrict__ sc = a.sc;
+    const long long nc = G.nc, nall = 9 * nc, si = (long long)G.jymax * G.kzmax;
+    unsigned c0 = 0, c1 = 0, c2 = 0;
+    T f[9];
+    if (live) {
+        face_flux_at<T, 0>(G, V, Vinit, sc, ia - 1, j, k, f);
+#pragma unroll
+        for (int m = 0; m < 9; m++) sm.fr[0][jj][m][lane] = f[m];
+    }
+    int lo = 0, b = 0;
+    for (int i = ia; i < ib; i++) {
+        if (w > 0) {
+            if (live) {
+                face_flux_at<T, 0>(G, V, Vinit, sc, i, j, k, f);
+#pragma unroll
+                for (int m = 0; m < 9; m++) sm.fr[lo ^ 1][jj][m][lane] = f[m];
+                face_flux_at<T, 1>(G, V, Vinit, sc, i, j, k, f);
+#pragma unroll
+                for (int m = 0; m < 9; m++) sm.fg[b][jj + 1][m][lane] = f[m];
+                face_flux_at<T, 2>(G, V, Vinit, sc, i, j, k, f);
+#pragma unroll
+                for (int m = 0; m < 9; m++) sm.fh[b][jj][m][lane + 1] = f[m];
+            }
+        } else {
+            /* next plane's cold inputs: U^n, U^(k), rhofloor rows of the
+             * tile, and the V plane the r reconstruction reaches next */
+            if (i + 1 < ib) {
+                const long long row0 = ((long long)(i + 1) * G.jymax + j0) * G.kzmax + k0;
+                for (int t = lane; t < 19 * TJ; t += 32) {
+                    const int v = t / TJ, r = t - v * TJ;
+                    if (j0 + r >= G.jymax - 1) continue;
+                    const long long e0 = row0 + (long long)r * G.kzmax;
+                    if (v < 9) prefetch_run<T>(a.Un, nall, v * nc + e0, v * nc + e0 + 32);
+                    else if (v < 18) { if (a.kind != 0) prefetch_run<T>(a.U1, nall, (v - 9) * nc + e0, (v - 9) * nc + e0 + 32); }
+                    else prefetch_run<T>(a.rhofloor, nc, e0, e0 + 32);
+                }
+            }
+            if (i + 3 < G.ixmax) {
+                const long long pl0 = (long long)(i + 3) * si;
+                for (int t = lane; t < 9 * (TJ + 4); t += 32) {
+                    const int v = t / (TJ + 4), jr = j0 - 2 + (t - v * (TJ + 4));
+                    if (jr < 0 || jr >= G.jymax) continue;
+                    const long long e0 = v * nc + pl0 + (long long)jr * G.kzmax;
+                    const int ka = max(k0 - 2, 0), kb = min(k0 + 34, G.kzmax);
+                    prefetch_run<T>(V, nall, e0 + ka, e0 + kb);
+                }
+            }
+            if (kin && j0 < G.jymax - 1) {
+                face_flux_at<T, 1>(G, V, Vinit, sc, i, j0 - 1, k, f);
+#pragma unroll
+                for (int m = 0; m < 9; m++) sm.fg[b][0][m][lane] = f[m];
+            }
+            if (lane < TJ && j0 + lane < G.jymax - 1 && k0 < G.kzmax - 1) {
+                face_flux_at<T, 2>(G, V, Vinit, sc, i, j0 + lane, k0 - 1, f);
+#pragma unroll
+                for (int m = 0; m < 9; m++) sm.fh[b][lane][m][0] = f[m];
+            }
+        }
+        __syncthreads();
+        if (live) {
+            T g[6], div[9];
+            geo_factors<T>(G, i, k, g);
+#pragma unroll
+            for (int m = 0; m < 9; m++)
+                div[m] = flux_div<T>(g, sm.fr[lo ^ 1][jj][m][lane], sm.fr[lo][jj][m][lane], sm.fg[b][jj + 1][m][lane],
+                                     sm.fg[b][jj][m][lane], sm.fh[b][jj][m][lane + 1], sm.fh[b][jj][m][lane]);
+            int flags = update_apply<T>(G, a, i, j, k, div);
+            c0 += flags & 1; c1 += (flags >> 1) & 1; c2 += (flags >> 2) & 1;
+        }
+        lo ^= 1;
+        b ^= 1;
+    }
+    add_counts3(c0, c1, c2, a.counters);
 }
 
 /* Ghost cell -> (source interior cell, sign flip mask) after the fill sequence
@@ -407,6 +595,22 @@ cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, co
                           Box b, bool reflayout, cudaStream_t st)
 {
     if (b.i1 <= b.i0 || b.j1 <= b.j0 || b.k1 <= b.k0) return cudaSuccess;
+    if (dir == 2) {
+        /* boundary z faces in their own launch, the rest below */
+        const int lo = b.k0 == 0, hi = b.k1 > G.kzmax - 2 && b.k0 <= G.kzmax - 2 && G.kzmax - 2 > 0;
+        if (lo || hi) {
+            long long n = (long long)(b.i1 - b.i0) * (b.j1 - b.j0) * (lo + hi);
+            if (reflayout)
+                flux_zedge_kernel<T, true><<<nblocks(n, 128), 128, 0, st>>>(G, V, Vinit, sc, F, b, lo, hi);
+            else
+                flux_zedge_kernel<T, false><<<nblocks(n, 128), 128, 0, st>>>(G, V, Vinit, sc, F, b, lo, hi);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        if (lo) b.k0 = 1;
+        if (hi) b.k1 = G.kzmax - 2;
+        if (b.k1 <= b.k0) return cudaSuccess;
+    }
     dim3 gr, bl;
     grid3(b.k1 - b.k0, b.j1 - b.j0, b.i1 - b.i0, gr, bl);
 #define MHD_FLUX_CASE(D, RL) flux_kernel<T, D, RL><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b)
@@ -438,6 +642,37 @@ cudaError_t launch_update_t(const Geom &G, const StageArgs<T> &a, cudaStream_t s
     dim3 gr, bl;
     grid3(G.kzmax - 2, G.jymax - 2, G.ixmax - 2, gr, bl);
     update_kernel<T><<<gr, bl, 0, st>>>(G, a);
+    return cudaGetLastError();
+}
+
+/* fused stage launcher: tile 32 (k) x tj (j) cells, runs of seg planes in i */
+template <typename T, int TJ>
+static cudaError_t stage_attr_t()
+{
+    constexpr int MINB = sizeof(T) == 4 ? 4 : 2;
+    return cudaFuncSetAttribute(stage_kernel<T, TJ, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(StageSmem<T, TJ>));
+}
+
+template <typename T>
+cudaError_t prepare_stage_t()
+{
+    return stage_attr_t<T, 7>();
+}
+
+template <typename T>
+cudaError_t launch_stage_t(const Geom &G, const StageArgs<T> &a, int tj, int seg, cudaStream_t st)
+{
+    if (seg < 1) seg = 1;
+    const int ni = G.ixmax - 2, nj = G.jymax - 2, nk = G.kzmax - 2;
+    constexpr int MINB = sizeof(T) == 4 ? 4 : 2;
+    dim3 gr((nk + 31) / 32, 0, (ni + seg - 1) / seg);
+    if (tj == 7) {
+        gr.y = (nj + 6) / 7;
+        stage_kernel<T, 7, MINB><<<gr, dim3(32, 8), sizeof(StageSmem<T, 7>), st>>>(G, a, seg);
+    } else {
+        return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 
@@ -500,6 +735,14 @@ cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream
     cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st)                           \
     {                                                                                                        \
         return launch_ghost_t<T>(G, a, st);                                                                  \
+    }                                                                                                        \
+    cudaError_t launch_stage(const Geom &G, const StageArgs<T> &a, int tj, int seg, cudaStream_t st)         \
+    {                                                                                                        \
+        return launch_stage_t<T>(G, a, tj, seg, st);                                                         \
+    }                                                                                                        \
+    cudaError_t prepare_stage(T *)                                                                           \
+    {                                                                                                        \
+        return prepare_stage_t<T>();                                                                         \
     }                                                                                                        \
     cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st)            \
     {                                                                                                        \

@@ -32,6 +32,7 @@ struct StageArgs {
     const float *trigf;
     int kind, last;
     int *counters;
+    const T *Vinit;        /* initial primitives (z MC boundary states; fused stage) */
 };
 
 #define MHD_DECLARE_LAUNCHERS(T)                                                                             \
@@ -41,6 +42,8 @@ struct StageArgs {
                               T *Vl, T *Vr, Box b, cudaStream_t st);                                         \
     cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                        \
     cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                         \
+    cudaError_t launch_stage(const Geom &G, const StageArgs<T> &a, int tj, int seg, cudaStream_t st);        \
+    cudaError_t prepare_stage(T *); /* shared-memory attribute of the fused kernels */                       \
     cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st);            \
     cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
                               const float *trigf, double *S, cudaStream_t st);                               \

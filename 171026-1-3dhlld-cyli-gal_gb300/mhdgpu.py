@@ -113,6 +113,7 @@ def lib():
         "mhd_batch_tune": (C.c_int, [vp, IP]),
         "mhd_upload_state": (C.c_int, [vp, vp, vp]),
         "mhd_prof_enable": (C.c_int, [vp, C.c_int]),
+        "mhd_set_stage_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
         "mhd_prof_read": (C.c_int, [vp, DP, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]),
         "mhd_launch_count": (C.c_longlong, [vp]),
         "mhd_timer_start": (C.c_int, [vp]),
@@ -367,16 +368,21 @@ class Disc:
     def download_into(self, U, V):
         check(lib().mhd_download(self.h, _ptr(U), _ptr(V)), "mhd_download")
 
-    PROF_KINDS = ["flux_r", "flux_phi", "flux_z", "update", "ghost", "setdt", "trig", "convert"]
+    PROF_KINDS = ["flux_r", "flux_phi", "flux_z", "update", "ghost", "setdt", "trig", "convert", "stage"]
 
     def prof(self, on=True):
         check(lib().mhd_prof_enable(self.h, 1 if on else 0), "mhd_prof_enable")
 
     def prof_read(self):
-        ms = np.zeros(8)
-        n = np.zeros(8, dtype=np.int64)
+        ms = np.zeros(len(self.PROF_KINDS))
+        n = np.zeros(len(self.PROF_KINDS), dtype=np.int64)
         check(lib().mhd_prof_read(self.h, ms, n), "mhd_prof_read")
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PROF_KINDS)}
+
+    def set_stage_shape(self, fused=True, tj=7, seg=32):
+        """fused: one kernel per stage for fluxes + update; tj (7) j-cells
+        per tile, seg r-cells per run (mhd_set_stage_shape)."""
+        check(lib().mhd_set_stage_shape(self.h, 1 if fused else 0, int(tj), int(seg)), "mhd_set_stage_shape")
 
     def launches(self):
         return int(lib().mhd_launch_count(self.h))
