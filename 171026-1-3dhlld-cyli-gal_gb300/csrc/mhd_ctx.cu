@@ -160,9 +160,14 @@ static int gather_ik(const double *src, int compact, int ni, int nj, int nk, int
 
 static void free_all(mhd_ctx *ctx)
 {
+    if (ctx->writer.joinable()) ctx->writer.join();
     void *dev[] = {ctx->dtab, ctx->ftab, ctx->U, ctx->U1, ctx->Va, ctx->Vb, ctx->Uinit, ctx->Vinit,
                    ctx->rhofloor, ctx->F, ctx->Gf, ctx->H, ctx->Uraw, ctx->d_sc, ctx->d_trig, ctx->d_trigf,
-                   ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run};
+                   ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run, ctx->d_snap};
+    if (ctx->h_snap) cudaFreeHost(ctx->h_snap);
+    if (ctx->ev_snap) cudaEventDestroy(ctx->ev_snap);
+    if (ctx->ev_host) cudaEventDestroy(ctx->ev_host);
+    if (ctx->st_io) cudaStreamDestroy(ctx->st_io);
     for (size_t q = 0; q < sizeof dev / sizeof dev[0]; q++)
         if (dev[q]) cudaFree(dev[q]);
     if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
@@ -267,6 +272,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
             dvol[(size_t)i * kzmax + k] = 0.5 * (g->xm[i] * g->xm[i] - g->xm[i - 1] * g->xm[i - 1]) * g->dy * g->dzm[k - 1];
     ctx->hx.assign(g->x, g->x + ixmax);
     ctx->hy.assign(g->y, g->y + jymax);
+    ctx->hz.assign(g->z, g->z + kzmax);
     ctx->hspL = spL;
     ctx->omdiff = p->omegapattern - p->omegasp;
 
@@ -831,6 +837,59 @@ extern "C" int mhd_run(mhd_ctx *ctx, int nsteps, double *t)
     CK(cudaStreamSynchronize(ctx->st));
     *t = h->t;
     return h->dtbad ? MHD_ERR_DT : MHD_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* asynchronous checkpoint (BinaryOutput, output.h:1202-1414)                */
+/* ------------------------------------------------------------------------ */
+extern "C" int mhd_checkpoint_wait(mhd_ctx *ctx)
+{
+    if (!ctx) return MHD_ERR_ARG;
+    if (ctx->writer.joinable()) ctx->writer.join();
+    int rc = ctx->ck_pending ? ctx->ck_status : MHD_OK;
+    ctx->ck_pending = 0;
+    return rc;
+}
+
+extern "C" int mhd_checkpoint_begin(mhd_ctx *ctx, const char *root, int nout, double t)
+{
+    if (!ctx || !root || nout < 0) return MHD_ERR_ARG;
+    if (!ctx->uploaded) return MHD_ERR_STATE;
+    int rc = mhd_checkpoint_wait(ctx);
+    if (rc) return rc;
+    const size_t n = 9 * (size_t)ctx->nc;
+    if (!ctx->d_snap) {
+        CK(cudaMalloc((void **)&ctx->d_snap, n * sizeof(double)));
+        cudaError_t e = cudaMallocHost((void **)&ctx->h_snap, n * sizeof(double));
+        if (e != cudaSuccess) {
+            cudaFree(ctx->d_snap);
+            ctx->d_snap = NULL;
+            ctx->h_snap = NULL;
+            ctx->last_cuda = e;
+            return MHD_ERR_NOMEM;
+        }
+        CK(cudaStreamCreateWithFlags(&ctx->st_io, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->ev_snap, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->ev_host, cudaEventDisableTiming | cudaEventBlockingSync));
+    }
+    /* snapshot on the step stream (ordered after the steps enqueued so far) */
+    if (ctx->fp32) LAUNCH(PK_CVT, launch_cvt_back((const float *)vcur_ptr(ctx), ctx->d_snap, (long long)n, ctx->st));
+    else CK(cudaMemcpyAsync(ctx->d_snap, vcur_ptr(ctx), n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaEventRecord(ctx->ev_snap, ctx->st));
+    /* device -> host on the I/O stream, beside the following steps */
+    CK(cudaStreamWaitEvent(ctx->st_io, ctx->ev_snap, 0));
+    CK(cudaMemcpyAsync(ctx->h_snap, ctx->d_snap, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st_io));
+    CK(cudaEventRecord(ctx->ev_host, ctx->st_io));
+    ctx->ck_pending = 1;
+    ctx->ck_status = MHD_OK;
+    std::string dir(root);
+    ctx->writer = std::thread([ctx, dir, nout, t]() {
+        cudaSetDevice(ctx->device);
+        if (cudaEventSynchronize(ctx->ev_host) != cudaSuccess) { ctx->ck_status = MHD_ERR_CUDA; return; }
+        ctx->ck_status = mhd_binary_output_arrays(dir.c_str(), nout, t, ctx->ix, ctx->jy, ctx->kz,
+                                                  ctx->hx.data(), ctx->hy.data(), ctx->hz.data(), ctx->h_snap);
+    });
+    return MHD_OK;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "mhd_launch.h"
@@ -35,7 +37,7 @@ struct mhd_ctx {
     int *d_cnt, *h_cnt;
     double *d_stage;
     long long stage_n;
-    std::vector<double> hx, hy, hspL;
+    std::vector<double> hx, hy, hz, hspL;
     double omdiff;
     int uploaded;
     cudaError_t last_cuda;
@@ -52,6 +54,12 @@ struct mhd_ctx {
     double prof_ms[MHD_PROF_NKIND];
     long long prof_n[MHD_PROF_NKIND];
     cudaEvent_t tev[2];
+    /* asynchronous checkpoint: device snapshot, pinned host copy, writer */
+    double *d_snap, *h_snap;
+    cudaStream_t st_io;
+    cudaEvent_t ev_snap, ev_host;
+    std::thread writer;
+    int ck_pending, ck_status;
 };
 
 #endif

@@ -17,6 +17,7 @@ LIBPATH = os.path.join(PKG, "lib", "libmhdgpu.so")
 MHD_OK = 0
 MHD_ERR_ARG = -1
 MHD_ERR_DT = -3
+MHD_ERR_IO = -8
 LIMITER = {"minmod": 0, "mc": 1}
 SOLVER = {"hlld": 0, "hll": 1}
 PREC = {"fp64": 0, "fp32": 1}
@@ -89,6 +90,16 @@ def lib():
         "mhd_ic_disc": (C.c_int, [C.POINTER(MhdGrid), C.c_double, C.c_double, C.c_ulonglong,
                                   C.c_double, vp, vp, vp, vp, vp]),
         "mhd_vtou": (C.c_int, [C.POINTER(MhdGrid), DP, DP]),
+        "mhd_binary_output": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.POINTER(MhdGrid), DP]),
+        "mhd_binary_output_arrays": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                               DP, DP, DP, DP]),
+        "mhd_restart_read": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, DP]),
+        "mhd_check": (C.c_int, [C.POINTER(MhdGrid), C.POINTER(MhdParams), DP, DP, DP, vp]),
+        "mhd_save_initial": (C.c_int, [C.POINTER(MhdGrid), C.c_double, DP, DP, vp, vp, vp]),
+        "mhd_restart": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.POINTER(MhdGrid), C.POINTER(MhdParams),
+                                  DP, DP, DP, DP, DP, _PD, _PD]),
+        "mhd_checkpoint_begin": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_double]),
+        "mhd_checkpoint_wait": (C.c_int, [vp]),
         "mhd_create": (C.c_int, [C.POINTER(MhdGrid), C.POINTER(MhdParams), C.POINTER(vp)]),
         "mhd_destroy": (None, [vp]),
         "mhd_upload": (C.c_int, [vp, vp, vp, vp, vp, vp]),
@@ -276,6 +287,48 @@ def oracle_params(params):
 # device context
 # ---------------------------------------------------------------------------
 
+def _path(root):
+    return os.fsencode(str(root))
+
+
+def binary_output(root, nout, t, grid, V):
+    """BinaryOutput() of V into <root>/<nout>/ (mhd_binary_output)."""
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    check(lib().mhd_binary_output(_path(root), int(nout), float(t), C.byref(grid.g), V), "mhd_binary_output")
+
+
+def restart_read(root, num, grid):
+    """V from the files of <root>/<num>/ (mhd_restart_read)."""
+    V = np.zeros((9,) + grid.cell)
+    check(lib().mhd_restart_read(_path(root), int(num), grid.ix, grid.jy, grid.kz, V), "mhd_restart_read")
+    return V
+
+
+def vtou(grid, V):
+    U = np.zeros((9,) + grid.cell)
+    check(lib().mhd_vtou(C.byref(grid.g), np.ascontiguousarray(V, dtype=np.float64), U), "mhd_vtou")
+    return U
+
+
+def check_floors(grid, params, U, V, rhofloor):
+    """Check() in place on U, V; returns the three floor counters."""
+    cnt = np.zeros(3, dtype=np.int32)
+    check(lib().mhd_check(C.byref(grid.g), C.byref(params), U, V, np.ascontiguousarray(rhofloor), _ptr(cnt)),
+          "mhd_check")
+    return cnt
+
+
+def restart(root, nout, tint, grid, params):
+    """The reference's restart sequence (mhd_restart): returns
+    U, V, Uinit, Vinit, rhofloor, t, tout."""
+    shp = (9,) + grid.cell
+    U, V, Ui, Vi, rf = np.zeros(shp), np.zeros(shp), np.zeros(shp), np.zeros(shp), np.zeros(grid.cell)
+    t, tout = C.c_double(), C.c_double()
+    check(lib().mhd_restart(_path(root), int(nout), float(tint), C.byref(grid.g), C.byref(params),
+                            U, V, Ui, Vi, rf, C.byref(t), C.byref(tout)), "mhd_restart")
+    return U, V, Ui, Vi, rf, t.value, tout.value
+
+
 class Disc:
     """One disc on the GPU: a thin wrapper over mhd_create/mhd_step/... ."""
 
@@ -378,6 +431,13 @@ class Disc:
         n = np.zeros(len(self.PROF_KINDS), dtype=np.int64)
         check(lib().mhd_prof_read(self.h, ms, n), "mhd_prof_read")
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PROF_KINDS)}
+
+    def checkpoint_begin(self, root, nout, t):
+        """Asynchronous BinaryOutput of the current V (mhd_checkpoint_begin)."""
+        check(lib().mhd_checkpoint_begin(self.h, _path(root), int(nout), float(t)), "mhd_checkpoint_begin")
+
+    def checkpoint_wait(self):
+        check(lib().mhd_checkpoint_wait(self.h), "mhd_checkpoint_wait")
 
     def set_stage_shape(self, fused=True, tj=7, seg=32):
         """fused: one kernel per stage for fluxes + update; tj (7) j-cells

@@ -135,6 +135,30 @@ int mhd_ic_disc(const mhd_grid *g, double beta, double amp, unsigned long long s
 /* VtoU() (vtou.h:20-62) on caller arrays. */
 int mhd_vtou(const mhd_grid *g, const double *V, double *U);
 
+/* ---- checkpoint files and restart (host, no GPU) ------------------------ */
+/* BinaryOutput() (output.h:1202-1414): directory <root>/<nout> holding
+ * GridTime.dat (text "%d\t%d\t%d\t%.3e" of ixmax, jymax, kzmax, t), the cell
+ * centres r, phi, z and V as raw FP64 files rho vr vphi vz br bphi bz pr psi,
+ * each [ixmax][jymax][kzmax] with ghosts.  root "." is the reference's own
+ * location.  The _arrays form takes the dimensions and the centre arrays. */
+int mhd_binary_output(const char *root, int nout, double t, const mhd_grid *g, const double *V);
+int mhd_binary_output_arrays(const char *root, int nout, double t, int ix, int jy, int kz, const double *x,
+                             const double *y, const double *z, const double *V);
+/* The file part of RestartRead() (restartread.h:9-121): V from <root>/<num>. */
+int mhd_restart_read(const char *root, int num, int ix, int jy, int kz, double *V);
+/* Check() (check.h:23-188) on caller arrays, every cell: density, pressure
+ * and plasma-beta floors; counters (may be NULL) = cells caught by each. */
+int mhd_check(const mhd_grid *g, const mhd_params *p, double *U, double *V, const double *rhofloor,
+              int counters[3]);
+/* SaveInitial() (saveinitial.h:18-50): Uinit=U, Vinit=V, rhofloor=rhocr*rho. */
+int mhd_save_initial(const mhd_grid *g, double rhocr, const double *U, const double *V, double *Uinit,
+                     double *Vinit, double *rhofloor);
+/* The restart branch of main.c:244-270: RestartRead(0) (VtoU + Check with
+ * zero floors), SaveInitial(), RestartRead(nout); t = nout*tint and
+ * tout = (nout+1)*tint.  Gravity tables are the caller's (InitialGravity). */
+int mhd_restart(const char *root, int nout, double tint, const mhd_grid *g, const mhd_params *p, double *U,
+                double *V, double *Uinit, double *Vinit, double *rhofloor, double *t, double *tout);
+
 /* ---- device context: the step ------------------------------------------- */
 int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out);
 void mhd_destroy(mhd_ctx *ctx);
@@ -170,6 +194,16 @@ void *mhd_stream(mhd_ctx *ctx);
 /* Upload only the evolving state U, V (same layout as mhd_upload); the
  * initial arrays and floors from the last mhd_upload stay. */
 int mhd_upload_state(mhd_ctx *ctx, const double *U, const double *V);
+
+/* Asynchronous BinaryOutput of the context's current V: the state is copied
+ * (as FP64) to a device snapshot on the context's stream, then to pinned host
+ * memory on a second stream, and a host thread writes <root>/<nout> once the
+ * copy lands -- the caller keeps stepping meanwhile.  One checkpoint is in
+ * flight at a time: begin waits for the previous one.  wait returns the
+ * writer's status (MHD_ERR_IO on a failed write).  Device and pinned memory
+ * for the snapshot (9 FP64 arrays each) are taken on the first call. */
+int mhd_checkpoint_begin(mhd_ctx *ctx, const char *root, int nout, double t);
+int mhd_checkpoint_wait(mhd_ctx *ctx);
 
 /* ---- instrumentation ------------------------------------------------------ */
 /* Per-kernel timing with CUDA events recorded around every launch on the

@@ -9,6 +9,9 @@ from the reference tree by ``-I``.  Outputs go only to ``oracle/_ref/``
 FP flags: ``-O2 -ffp-contract=off`` so no multiply-add is fused (the GPU plain
 FP64 build uses ``--fmad=false`` for the same reason); ``-mcmodel=medium``
 because the reference's static arrays exceed 2 GB at 256x256x128.
+``-Wl,-Bsymbolic`` binds the reference's globals to its own definitions: it
+declares ``char dirname[64]`` (commontemp.h:183), which inside a shared object
+would otherwise resolve to the C library's ``dirname()`` function.
 """
 import os
 import subprocess
@@ -36,10 +39,11 @@ def build(nr, nphi, nz, force=False):
     src = os.path.join(HERE, "ref_harness.c")
     inp = os.path.join(HERE, "input.h")
     if (not force and os.path.exists(out)
-            and os.path.getmtime(out) >= max(os.path.getmtime(src), os.path.getmtime(inp))):
+            and os.path.getmtime(out) >= max(os.path.getmtime(src), os.path.getmtime(inp),
+                                              os.path.getmtime(os.path.abspath(__file__)))):
         return out
     cmd = ["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
-           "-fPIC", "-shared", "-mcmodel=medium",
+           "-fPIC", "-shared", "-mcmodel=medium", "-Wl,-Bsymbolic",
            "-w", "-Wno-implicit-function-declaration",
            "-DREF_NR=%d" % nr, "-DREF_NPHI=%d" % nphi, "-DREF_NZ=%d" % nz,
            "-I", HERE, "-I", REFERENCE_TREE, src, "-o", out + ".tmp", "-lm"]

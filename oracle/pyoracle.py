@@ -263,6 +263,8 @@ class RefOracle(_Common):
         lib.ref_set_threads.argtypes = [C.c_int]
         lib.ref_set_threads(1)
         lib.ref_binary_output.argtypes = [C.c_int, C.c_double]
+        lib.ref_restart_read.argtypes = [C.c_int]
+        lib.ref_check_flags.argtypes = [_IP]
         self.lib = lib
         self.rhocr = float(params["rhocr"])
         p = np.array([float(params[f]) for f in PARAM_FIELDS])
@@ -286,6 +288,28 @@ class RefOracle(_Common):
 
     def close(self):
         pass
+
+    def binary_output(self, num, t):
+        """BinaryOutput() into ./<num>/ of the current working directory."""
+        self.lib.ref_binary_output(int(num), float(t))
+
+    def restart_read(self, num):
+        """RestartRead(num) from ./<num>/: V from the files, VtoU, Check;
+        returns Check's floor counters."""
+        self.lib.ref_set_threads(1)
+        self.lib.ref_restart_read(int(num))
+        cnt = np.zeros(3, dtype=np.int32)
+        self.lib.ref_check_flags(cnt)
+        return cnt
+
+    def save_initial(self):
+        self.lib.ref_save_initial()
+
+    def get_initial(self):
+        shp = (9,) + self.cell
+        Ui, Vi, rf = np.zeros(shp), np.zeros(shp), np.zeros(self.cell)
+        self.lib.ref_get_initial(Ui, Vi, rf)
+        return Ui, Vi, rf
 
     def initial_gravity(self):
         self.lib.ref_initial_gravity()

@@ -161,6 +161,8 @@ void ref_reset(void)
 	memset(Vl, 0, sizeof Vl); memset(Vr, 0, sizeof Vr); memset(Ul, 0, sizeof Ul); memset(Ur, 0, sizeof Ur);
 	memset(Fl, 0, sizeof Fl); memset(Fr, 0, sizeof Fr); memset(Gl, 0, sizeof Gl); memset(Gr, 0, sizeof Gr);
 	memset(Hl, 0, sizeof Hl); memset(Hr, 0, sizeof Hr);
+	memset(Uinitial, 0, sizeof Uinitial); memset(Vinitial, 0, sizeof Vinitial);
+	memset(rhofloor, 0, sizeof rhofloor);
 	dt = 0.0; ch = 0.0; t = 0.0; psicoef = 0.0;
 }
 
@@ -325,4 +327,13 @@ void ref_binary_output(int num, double tnow)
 {
 	nout = num; t = tnow;
 	BinaryOutput();
+}
+
+/* RestartRead(num) (restartread.h:9-143): V from ./<num>/, VtoU, Check */
+void ref_restart_read(int num) { RestartRead(num); }
+
+/* floor counters of the last Check() */
+void ref_check_flags(int *out)
+{
+	out[0] = rhoflag; out[1] = prflag; out[2] = oneobetaflag;
 }
