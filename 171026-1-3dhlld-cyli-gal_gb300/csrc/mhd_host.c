@@ -220,31 +220,49 @@ int mhd_grid_build(const mhd_gridspec *s, double *st, mhd_grid *g)
     return MHD_OK;
 }
 
-/* initialgravity.h:22-79 (v0 = 6.558e+6, constant.h:78) */
+/* The fixed axisymmetric potential's parameters (initialgravity.h:34-36,
+ * model.h:162-164): logarithmic dark halo (vhalo0, dh), Miyamoto-Nagai disc
+ * (a, b, md), Hernquist bulge (db, mb); v0 = 6.558e+6 (constant.h:84). */
+static const double GV_VHALO0 = 131.5e+5 / 6.558e+6, GV_DH = 1.2;
+static const double GV_A = 0.65, GV_B = 0.026, GV_MD = 10.0;
+static const double GV_DB = 0.07, GV_MB = 3.4;
+
+/* radial and vertical axisymmetric gravity at (x, z): initialgravity.h:52-70,
+ * model.h:229-246 (the two spell the same expressions) */
+static double axi_grx(double x, double z)
+{
+    const double vhalo0 = GV_VHALO0, dh = GV_DH, a = GV_A, b = GV_B, md = GV_MD, db = GV_DB, mb = GV_MB;
+    double x2 = x * x, z2 = z * z;
+    return ((-2.0 * vhalo0 * vhalo0 / (x2 + z2 + dh * dh)
+             - md / pow(x2 + (a + sqrt(z2 + b * b)) * (a + sqrt(z2 + b * b)), 1.5)
+             - mb / ((sqrt(x2 + z2) + db) * (sqrt(x2 + z2) + db) * sqrt(x2 + z2)))
+            * x);
+}
+
+static double axi_grz(double x, double z)
+{
+    const double vhalo0 = GV_VHALO0, dh = GV_DH, a = GV_A, b = GV_B, md = GV_MD, db = GV_DB, mb = GV_MB;
+    double x2 = x * x, z2 = z * z;
+    return ((-2.0 * vhalo0 * vhalo0 / (x2 + z2 + dh * dh)
+             - md / pow(x2 + (a + sqrt(z2 + b * b)) * (a + sqrt(z2 + b * b)), 1.5)
+               * (1.0 + a / sqrt(z2 + b * b))
+             - mb / ((sqrt(x2 + z2) + db) * (sqrt(x2 + z2) + db) * sqrt(x2 + z2)))
+            * z);
+}
+
+/* initialgravity.h:22-79 */
 int mhd_initial_gravity(const mhd_grid *g, double *grx, double *gry, double *grz)
 {
     if (!g || !grx || !gry || !grz) return MHD_ERR_ARG;
-    const double vhalo0 = 131.5e+5 / 6.558e+6, dh = 1.2;
-    const double a = 0.65, b = 0.026, md = 10.0;
-    const double db = 0.07, mb = 3.4;
     int ixmax = g->ix + 2, jymax = g->jy + 2, kzmax = g->kz + 2;
     int nj = g->compact ? 1 : jymax;
     for (int i = 0; i < ixmax; i++)
         for (int j = 0; j < nj; j++)
             for (int k = 0; k < kzmax; k++) {
-                double x2 = g->x[i] * g->x[i];
-                double z2 = g->z[k] * g->z[k];
                 size_t q = ((size_t)i * nj + j) * kzmax + k;
-                grx[q] = ((-2.0 * vhalo0 * vhalo0 / (x2 + z2 + dh * dh)
-                           - md / pow(x2 + (a + sqrt(z2 + b * b)) * (a + sqrt(z2 + b * b)), 1.5)
-                           - mb / ((sqrt(x2 + z2) + db) * (sqrt(x2 + z2) + db) * sqrt(x2 + z2)))
-                          * g->x[i]);
+                grx[q] = axi_grx(g->x[i], g->z[k]);
                 gry[q] = 0.0;
-                grz[q] = ((-2.0 * vhalo0 * vhalo0 / (x2 + z2 + dh * dh)
-                           - md / pow(x2 + (a + sqrt(z2 + b * b)) * (a + sqrt(z2 + b * b)), 1.5)
-                             * (1.0 + a / sqrt(z2 + b * b))
-                           - mb / ((sqrt(x2 + z2) + db) * (sqrt(x2 + z2) + db) * sqrt(x2 + z2)))
-                          * g->z[k]);
+                grz[q] = axi_grz(g->x[i], g->z[k]);
             }
     return MHD_OK;
 }
@@ -331,5 +349,96 @@ int mhd_ic_disc(const mhd_grid *g, double beta, double amp, unsigned long long s
     }
     if (Vinit) memcpy(Vinit, Vw, 9 * nc * sizeof(double));
     if (!V) free(Vw);
+    return MHD_OK;
+}
+
+/* GalacticDisc3() (model.h:149-327): isothermal exponential gas disc
+ * (exp(-R/rdisc) in the midplane, hydrostatic in z) plus a hydrostatic
+ * isothermal halo in the fixed potential, rotation from radial balance in
+ * the frame rotating at omegasp, toroidal field of plasma beta 1e4 at R=0.
+ * Then VtoU, the z=0 symmetry fills of U (ZLeftVzAntisymBSymBoundary then
+ * ZLeftFreeBoundary, zboundary.h:67-96,170-190) and SaveInitial.  The
+ * reference evaluates the potentials in an OpenMP region, so the constant
+ * terms are computed at run time here too (through volatile reads) rather
+ * than folded by the compiler. */
+int mhd_ic_galactic_disc3(const mhd_grid *g, const mhd_params *p, double *U, double *V, double *Uinit,
+                          double *Vinit, double *rhofloor)
+{
+    if (!g || !p || !U || !V) return MHD_ERR_ARG;
+    const size_t ixmax = (size_t)g->ix + 2, jymax = (size_t)g->jy + 2, kzmax = (size_t)g->kz + 2;
+    const size_t nc = ixmax * jymax * kzmax;
+    /* constant.h:48-84 */
+    const double kpc = 3.08568e+21, mp = 1.673e-24, msun = 1.989e+33, v0 = 6.558e+6;
+    const double l0 = (10 * kpc);
+    volatile double pi4_v = 4.0 * M_PI;
+    const double pi4 = pi4_v;
+    volatile double knobs[7] = {GV_VHALO0, GV_DH, GV_A, GV_B, GV_MD, GV_DB, GV_MB};
+    const double vhalo0 = knobs[0], dh = knobs[1], a = knobs[2], b = knobs[3], md = knobs[4], db = knobs[5],
+                 mb = knobs[6];
+    /* model.h:179-201 */
+    const double mdisc = 0.4 * 0.75;
+    const double rdisc = 0.7, zdisc = 0.03;
+    const double discrho0 = (1.0e+10 * msun / (mp * 1000 * kpc * kpc * kpc) * mdisc / (pi4 * rdisc * rdisc * zdisc));
+    const double csdisc2 = 1.33e+8 * 1.0e+4 / (v0 * v0);
+    const double discbeta = 1.0e+4;
+    const double halorho0 = 1.0e-4 * (1.0e+10 * msun / (mp * 1000 * kpc * kpc * kpc) * mdisc
+                                      / (pi4 * rdisc * rdisc * zdisc));
+    const double cshalo2 = 1.33e+8 * 2.4e+6 / (v0 * v0);
+    const double oneocshalo2 = 1.0 / cshalo2;
+    const double oneocsdisc2 = 1.0 / csdisc2;
+    const double discbphi0 = sqrt(2.0 * csdisc2 * discrho0 / discbeta);
+    const double omegasp = p->omegasp;
+    for (size_t i = 0; i < ixmax; i++) {
+        const double xi = g->x[i];
+        for (size_t j = 0; j < jymax; j++)
+            for (size_t k = 0; k < kzmax; k++) {
+                const size_t q = (i * jymax + j) * kzmax + k;
+                const double zk = g->z[k];
+                const double x2 = xi * xi, z2 = zk * zk;
+                /* model.h:214-227 */
+                double potaxi = ((vhalo0 * vhalo0 * (2.0 * log(l0) + log(x2 + z2 + dh * dh)))
+                                 - md / sqrt(x2 + (a + sqrt(z2 + b * b)) * (a + sqrt(z2 + b * b)))
+                                 - mb / (sqrt(x2 + z2) + db));
+                double potaxir = ((vhalo0 * vhalo0 * (2.0 * log(l0) + log(x2 + dh * dh)))
+                                  - md / sqrt(x2 + (a + b) * (a + b))
+                                  - mb / (xi + db));
+                double potaxi0 = ((vhalo0 * vhalo0 * (2.0 * log(l0) + log(dh * dh)))
+                                  - md / (a + b)
+                                  - mb / db);
+                double grx = axi_grx(xi, zk);
+                /* model.h:251-293 */
+                double halorho = halorho0 * exp(-oneocshalo2 * (potaxi - potaxi0));
+                double halopr = cshalo2 * halorho;
+                double discrho = (discrho0 * exp(-xi / rdisc) * exp(-oneocsdisc2 * (potaxi - potaxir)));
+                double discpr = csdisc2 * discrho;
+                double rho = discrho + halorho;
+                V[q] = rho;
+                V[nc + q] = 0.0;
+                V[2 * nc + q] = (sqrt(-xi * (grx + csdisc2 / rdisc)) * discrho / rho - omegasp * xi);
+                V[3 * nc + q] = 0.0;
+                V[4 * nc + q] = 0.0;
+                V[5 * nc + q] = (discbphi0 * exp(-xi / rdisc) / (cosh(zk / zdisc) * cosh(zk / zdisc)));
+                V[6 * nc + q] = 0.0;
+                V[7 * nc + q] = discpr + halopr;
+                V[8 * nc + q] = 0.0;
+            }
+    }
+    int rc = mhd_vtou(g, V, U);
+    if (rc) return rc;
+    /* zboundary.h:67-96 then :170-190 on U: k=0 <- k=2 (v_z odd), U3 at k=1 = 0,
+     * then k=0 <- k=1 */
+    for (size_t i = 0; i < ixmax; i++)
+        for (size_t j = 0; j < jymax; j++) {
+            const size_t q0 = (i * jymax + j) * kzmax;
+            for (int m = 0; m < 9; m++)
+                U[m * nc + q0] = (m == 3) ? -U[m * nc + q0 + 2] : U[m * nc + q0 + 2];
+            U[3 * nc + q0 + 1] = 0.0;
+            for (int m = 0; m < 9; m++) U[m * nc + q0] = U[m * nc + q0 + 1];
+        }
+    /* saveinitial.h:27-45 */
+    if (Uinit) memcpy(Uinit, U, 9 * nc * sizeof(double));
+    if (Vinit) memcpy(Vinit, V, 9 * nc * sizeof(double));
+    if (rhofloor)
+        for (size_t q = 0; q < nc; q++) rhofloor[q] = U[q] * p->rhocr;
     return MHD_OK;
 }

@@ -90,6 +90,7 @@ def lib():
         "mhd_ic_disc": (C.c_int, [C.POINTER(MhdGrid), C.c_double, C.c_double, C.c_ulonglong,
                                   C.c_double, vp, vp, vp, vp, vp]),
         "mhd_vtou": (C.c_int, [C.POINTER(MhdGrid), DP, DP]),
+        "mhd_ic_galactic_disc3": (C.c_int, [C.POINTER(MhdGrid), C.POINTER(MhdParams), vp, vp, vp, vp, vp]),
         "mhd_binary_output": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.POINTER(MhdGrid), DP]),
         "mhd_binary_output_arrays": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                                DP, DP, DP, DP]),
@@ -202,9 +203,17 @@ class Grid:
         return cls(s)
 
     @classmethod
-    def shipped(cls):
+    def shipped(cls, nr=None, nphi=None, nz=None):
+        """The reference's stretched grid (input.h:45-76: 240x64x200); other
+        cell counts keep its spacing and stretching rules."""
         s = MhdGridSpec()
         check(lib().mhd_gridspec_shipped(C.byref(s)), "mhd_gridspec_shipped")
+        if nr:
+            s.ix = nr
+        if nphi:
+            s.jy = nphi
+        if nz:
+            s.kz = nz
         return cls(s)
 
     def arr(self, name, n):
@@ -228,6 +237,14 @@ class Grid:
             for n in range(3):
                 out[n] = self._grav[n].reshape(self.ixmax, 1, self.kzmax)
         return out
+
+    def ic_galactic_disc3(self, params):
+        """GalacticDisc3 (mhd_ic_galactic_disc3): U, V, Uinit, Vinit, rhofloor."""
+        shp = (9,) + self.cell
+        U, V, Ui, Vi, rf = np.zeros(shp), np.zeros(shp), np.zeros(shp), np.zeros(shp), np.zeros(self.cell)
+        check(lib().mhd_ic_galactic_disc3(C.byref(self.g), C.byref(params), _ptr(U), _ptr(V), _ptr(Ui), _ptr(Vi),
+                                          _ptr(rf)), "mhd_ic_galactic_disc3")
+        return U, V, Ui, Vi, rf
 
     def ic_disc(self, beta, amp=0.01, seed=0, rhocr=1.0e-4):
         U = np.zeros((9,) + self.cell)

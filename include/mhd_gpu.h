@@ -132,6 +132,14 @@ int mhd_initial_gravity(const mhd_grid *g, double *grxaxi, double *gryaxi, doubl
 int mhd_ic_disc(const mhd_grid *g, double beta, double amp, unsigned long long seed,
                 double rhocr, double *U, double *V, double *Uinit, double *Vinit,
                 double *rhofloor);
+/* GalacticDisc3() (model.h:149-327), the reference's shipped initial model:
+ * exponential isothermal gas disc + hydrostatic halo in the fixed potential
+ * of mhd_initial_gravity(), rotating in the omegasp frame, toroidal field;
+ * VtoU, the z=0 symmetry fills of U, SaveInitial.  Pair it with
+ * mhd_gridspec_shipped() and mhd_initial_gravity() (the potential it assumes).
+ * Uinit, Vinit, rhofloor may be NULL. */
+int mhd_ic_galactic_disc3(const mhd_grid *g, const mhd_params *p, double *U, double *V, double *Uinit,
+                          double *Vinit, double *rhofloor);
 /* VtoU() (vtou.h:20-62) on caller arrays. */
 int mhd_vtou(const mhd_grid *g, const double *V, double *U);
 

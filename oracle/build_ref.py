@@ -26,16 +26,17 @@ def available():
     return os.path.isfile(os.path.join(REFERENCE_TREE, "hlldx.h"))
 
 
-def lib_path(nr, nphi, nz):
-    return os.path.join(OUT, "libref_%dx%dx%d.so" % (nr, nphi, nz))
+def lib_path(nr, nphi, nz, shipped=False):
+    return os.path.join(OUT, "libref_%s%dx%dx%d.so" % ("shipped_" if shipped else "", nr, nphi, nz))
 
 
-def build(nr, nphi, nz, force=False):
-    """Build (if needed) and return the path of the reference library for one grid."""
+def build(nr, nphi, nz, force=False, shipped=False):
+    """Build (if needed) and return the path of the reference library for one
+    grid: the uniform disc grid, or (shipped) the reference's stretched grid."""
     if not available():
         raise FileNotFoundError("reference tree not present: %s" % REFERENCE_TREE)
     os.makedirs(OUT, exist_ok=True)
-    out = lib_path(nr, nphi, nz)
+    out = lib_path(nr, nphi, nz, shipped)
     src = os.path.join(HERE, "ref_harness.c")
     inp = os.path.join(HERE, "input.h")
     if (not force and os.path.exists(out)
@@ -45,8 +46,10 @@ def build(nr, nphi, nz, force=False):
     cmd = ["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
            "-fPIC", "-shared", "-mcmodel=medium", "-Wl,-Bsymbolic",
            "-w", "-Wno-implicit-function-declaration",
-           "-DREF_NR=%d" % nr, "-DREF_NPHI=%d" % nphi, "-DREF_NZ=%d" % nz,
-           "-I", HERE, "-I", REFERENCE_TREE, src, "-o", out + ".tmp", "-lm"]
+           "-DREF_NR=%d" % nr, "-DREF_NPHI=%d" % nphi, "-DREF_NZ=%d" % nz]
+    if shipped:
+        cmd.append("-DREF_SHIPPED")
+    cmd += ["-I", HERE, "-I", REFERENCE_TREE, src, "-o", out + ".tmp", "-lm"]
     subprocess.check_call(cmd)
     os.replace(out + ".tmp", out)
     return out

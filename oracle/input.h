@@ -13,7 +13,8 @@
  * to.
  *
  * Grid: the uniform cylindrical disc grid r in [0.1,1.5], phi in [0,2pi),
- * z in [-0.5,0.5].  The reference builds the grid with x[0]=x0-dx0 and
+ * z in [-0.5,0.5]; with -DREF_SHIPPED the reference's own stretched grid at
+ * the given size (its input.h uses 240x64x200).  The reference builds the grid with x[0]=x0-dx0 and
  * x[i+1]=x[i]+dx[i] (cylindricalgrid.h:36-47), so the first interior centre is
  * x0; stretching is disabled by putting lx/lz beyond the domain.
  */
@@ -26,6 +27,19 @@
 #define jy REF_NPHI
 #define kz REF_NZ
 
+#ifdef REF_SHIPPED
+/* the reference's own stretched grid (input.h:48-72): uniform dx0 up to
+ * r = lx and dz0 up to z = lz, then cells growing by stretchratio to at most
+ * 50 dx0 / 50 dz0; z starts at the midplane */
+#define lx 2.0
+#define ly pi2
+#define lz 0.03
+#define dx0 0.01
+#define dz0 0.0003
+#define x0 0.04
+#define y0 0.0
+#define z0 0.0
+#else
 #define lx 1.0e30
 #define ly pi2
 #define lz 1.0e30
@@ -34,6 +48,7 @@
 #define x0 (0.1+0.5*dx0)
 #define y0 0.0
 #define z0 (-0.5+0.5*dz0)
+#endif
 #define stretchratio 1.05
 #define rin 0.1
 

@@ -234,9 +234,9 @@ class Oracle(_Common):
 class RefOracle(_Common):
     """The reference's own C, compiled in place (oracle/_ref/, this container only)."""
 
-    def __init__(self, nr, nphi, nz, params):
+    def __init__(self, nr, nphi, nz, params, shipped=False):
         import build_ref  # noqa: local module in oracle/
-        path = build_ref.build(nr, nphi, nz)
+        path = build_ref.build(nr, nphi, nz, shipped=shipped)
         lib = C.CDLL(path, mode=C.RTLD_LOCAL)
         vp = None
         lib.ref_dims.argtypes = [_IP]
@@ -304,6 +304,11 @@ class RefOracle(_Common):
 
     def save_initial(self):
         self.lib.ref_save_initial()
+
+    def galactic_disc3(self):
+        """GalacticDisc3() (model.h:149-327): sets V, U, the initial arrays and
+        the axisymmetric gravity in the reference's globals."""
+        self.lib.ref_galactic_disc3()
 
     def get_initial(self):
         shp = (9,) + self.cell

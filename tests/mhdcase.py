@@ -74,3 +74,14 @@ def diagnostics_np(grid, U):
             + (bz[1:-1, 1:-1, 2:] - bz[1:-1, 1:-1, :-2]) / (z[2:] - z[:-2])[None, None, :])
     out["maxdivb"] = float(np.abs(divb).max())
     return out
+
+
+def make_shipped(M, dims=None, **over):
+    """The reference's shipped production case: its stretched grid (240x64x200,
+    or other cell counts with the same spacing rules), GalacticDisc3, the
+    reference's own knobs (live RK2, minmod, HLLD, spiral gravity, cooling)."""
+    grid = M.Grid.shipped(*(dims or (None, None, None)))
+    grid.set_initial_gravity()
+    params = M.default_params(**over)
+    U, V, Ui, Vi, rf = grid.ic_galactic_disc3(params)
+    return grid, params, U, V, Ui, Vi, rf
