@@ -18,7 +18,7 @@ MHD_OK = 0
 MHD_ERR_ARG = -1
 MHD_ERR_DT = -3
 MHD_ERR_IO = -8
-LIMITER = {"minmod": 0, "mc": 1}
+LIMITER = {"minmod": 0, "mc": 1, "vanleer": 2, "superbee": 3}
 SOLVER = {"hlld": 0, "hll": 1}
 PREC = {"fp64": 0, "fp32": 1}
 

@@ -44,6 +44,8 @@ extern "C" {
 /* ---- scheme choices ---------------------------------------------------- */
 #define MHD_LIMITER_MINMOD 0  /* MinmodLimiterX/Y/Z (limiterx.h:32, limitery.h:33, limiterz.h:30) */
 #define MHD_LIMITER_MC 1      /* MCLimiterX/Y/Z (limiterx.h:335, limitery.h:197, limiterz.h:294) */
+#define MHD_LIMITER_VANLEER 2 /* VanLeerLimiterX/Y/Z (limiterx.h:266, limitery.h:129, limiterz.h:232) */
+#define MHD_LIMITER_SUPERBEE 3 /* SuperbeeLimiterX/Y/Z (limiterx.h:394, limitery.h:256, limiterz.h:367) */
 #define MHD_SOLVER_HLLD 0     /* HLLDX/Y/Z (hlldx.h:28, hlldy.h:30, hlldz.h:28) */
 #define MHD_SOLVER_HLL 1      /* HLLX/Y/Z (hllx.h:29, hlly.h:29, hllz.h:26) */
 #define MHD_SCHEME_RK2 2      /* live TVDRK: Halfstep + Fullstep (tvdrungekutta.h:31-41) */

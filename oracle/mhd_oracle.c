@@ -556,6 +556,80 @@ static void mc_limiter(orc_ctx *o, int dir)
     }
 }
 
+/* van Leer (limiterx.h:266-326, limitery.h:129-188, limiterz.h:232-285) and
+ * superbee (limiterx.h:394-449, limitery.h:256-311, limiterz.h:367-432) */
+static void vl_sb_limiter(orc_ctx *o, int dir, int superbee)
+{
+    const double *V = o->V;
+    int ilo = dir == 0 ? 1 : 0, jlo = dir == 1 ? 1 : 0, klo = dir == 2 ? 1 : 0;
+    int ihi = o->ixmax - 1, jhi = o->jymax - 1, khi = o->kzmax - 1;
+    size_t st = dir == 0 ? (size_t)o->jymax * o->kzmax : dir == 1 ? (size_t)o->kzmax : 1;
+    int m;
+#pragma omp parallel for
+    for (m = 0; m < 9; m++) {
+        const double *vm = V + (size_t)m * o->nc;
+        double *vl = o->Vl + (size_t)m * o->nc, *vr = o->Vr + (size_t)m * o->nc;
+        for (int i = ilo; i < ihi; i++)
+            for (int j = jlo; j < jhi; j++)
+                for (int k = klo; k < khi; k++) {
+                    size_t q = IDX(o, i, j, k);
+                    double a = vm[q] - vm[q - st];
+                    double b = vm[q + st] - vm[q];
+                    double grad;
+                    if (a * b <= 0.0) grad = 0.0;
+                    else if (!superbee) grad = a * b / (a + b);
+                    else if (fabs(a) >= fabs(b)) grad = (a > 0.0) ? rmin(a, 2.0 * b) : rmax(a, 2.0 * b);
+                    else grad = (a > 0.0) ? rmin(2.0 * a, b) : rmax(2.0 * a, b);
+                    if (superbee) grad = 0.5 * grad;
+                    vl[q] = vm[q] + grad;
+                    vr[q - st] = vm[q] - grad;
+                }
+    }
+}
+
+/* the free fill of one direction (xvlrboundary.h:189-214 and the y, z
+ * analogues): Vl of the first face <- its Vr, Vr of the last face <- its Vl */
+static void vlr_free(orc_ctx *o, int dir)
+{
+    int n[3] = {o->ixmax - 1, o->jymax - 1, o->kzmax - 1};
+    int last = n[dir] - 1, m;
+#pragma omp parallel for
+    for (m = 0; m < 9; m++)
+        for (int i = 0; i < n[0]; i++)
+            for (int j = 0; j < n[1]; j++)
+                for (int k = 0; k < n[2]; k++) {
+                    int c = dir == 0 ? i : dir == 1 ? j : k;
+                    if (c == 0) A4(o, o->Vl, m, i, j, k) = A4(o, o->Vr, m, i, j, k);
+                    if (c == last) A4(o, o->Vr, m, i, j, k) = A4(o, o->Vl, m, i, j, k);
+                }
+}
+
+/* YVlrInitializeBoundary (yvlrboundary.h:26-52) */
+static void vlr_initialize_y(orc_ctx *o)
+{
+    int ixmax1 = o->ixmax - 1, jymax1 = o->jymax - 1, kzmax1 = o->kzmax - 1, m;
+#pragma omp parallel for
+    for (m = 0; m < 9; m++)
+        for (int i = 0; i < ixmax1; i++)
+            for (int k = 0; k < kzmax1; k++) {
+                A4(o, o->Vl, m, i, 0, k) = A4(o, o->Vinit, m, i, 0, k);
+                A4(o, o->Vr, m, i, jymax1 - 1, k) = A4(o, o->Vinit, m, i, jymax1, k);
+            }
+}
+
+/* the periodic fill along z (zvlrboundary.h:101-126) */
+static void vlr_periodic_z(orc_ctx *o)
+{
+    int ixmax1 = o->ixmax - 1, jymax1 = o->jymax - 1, kzmax1 = o->kzmax - 1, m;
+#pragma omp parallel for
+    for (m = 0; m < 9; m++)
+        for (int i = 0; i < ixmax1; i++)
+            for (int j = 0; j < jymax1; j++) {
+                A4(o, o->Vl, m, i, j, 0) = A4(o, o->Vl, m, i, j, kzmax1 - 1);
+                A4(o, o->Vr, m, i, j, kzmax1 - 1) = A4(o, o->Vr, m, i, j, 0);
+            }
+}
+
 /* left/right state boundaries applied inside the limiters:
  * x: XVlrPeriodicBoundary (xvlrboundary.h:153-180, limiterx.h:252,380)
  * y: YVlrPeriodicBoundary (yvlrboundary.h:61-87, limitery.h:108,242)
@@ -607,6 +681,21 @@ static void vlr_boundary(orc_ctx *o, int dir)
 
 static void limiter(orc_ctx *o, int dir)
 {
+    if (o->p.limiter == 2) {
+        /* van Leer: free in x (limiterx.h:314), periodic then initialize in y
+         * (limitery.h:176,183), free in z (limiterz.h:273) */
+        vl_sb_limiter(o, dir, 0);
+        if (dir == 1) { vlr_boundary(o, 1); vlr_initialize_y(o); }
+        else vlr_free(o, dir);
+        return;
+    }
+    if (o->p.limiter == 3) {
+        /* superbee: periodic in x, y, z (limiterx.h:444, limitery.h:306, limiterz.h:419) */
+        vl_sb_limiter(o, dir, 1);
+        if (dir == 2) vlr_periodic_z(o);
+        else vlr_boundary(o, dir);
+        return;
+    }
     if (o->p.limiter == 0) minmod_limiter(o, dir);
     else mc_limiter(o, dir);
     vlr_boundary(o, dir);

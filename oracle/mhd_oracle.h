@@ -36,7 +36,7 @@ typedef struct {
     double cfl, dtmin, rhocr, prcr, betacr;
     double epssp0, tausp, scalez, scaler, scalephase, armnum;
     double omegasp, omegapattern, pitch;
-    int limiter;   /* 0 minmod (limiterx.h:32), 1 MC (limiterx.h:335) */
+    int limiter;   /* 0 minmod (limiterx.h:32), 1 MC (limiterx.h:335), 2 van Leer (:266), 3 superbee (:394) */
     int solver;    /* 0 HLLD (hlldx.h:28), 1 HLL (hllx.h:29) */
     int scheme;    /* 2 live RK2 (halfstep/fullstep), 3 RK3 (first/second/thirdstep) */
     int cooling;   /* 0 off, 1 cooling.h:22 */

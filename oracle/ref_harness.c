@@ -11,8 +11,8 @@
  *     spiralgravity.h:39, never defined), Cooling() (setdt.h:54), Check()
  *     (halfstep.h:163);
  *   - run-time variant selection by redirecting the names the stage functions
- *     call (halfstep.h:40-77, firststep.h:37-78): minmod or MC limiter, HLLD or
- *     HLL solver;
+ *     call (halfstep.h:40-77, firststep.h:37-78): minmod, MC, van Leer or
+ *     superbee limiter, HLLD or HLL solver;
  *   - a cooling on/off switch in front of Cooling() (cooling.h:22);
  *   - TVD-RK3 driven exactly as the commented block of tvdrungekutta.h:21,63-83
  *     (psi factor exp(-dt*ch/cr/3), then FirstStep, SecondStep, ThirdStep);
@@ -80,15 +80,27 @@ int InitialGravity(void);
 #include "hllz.h"
 
 /* ---- run-time variant selection ------------------------------------------ */
-static int g_limiter = 0;   /* 0 minmod, 1 MC */
+static int g_limiter = 0;   /* 0 minmod, 1 MC, 2 van Leer, 3 superbee */
 static int g_solver = 0;    /* 0 HLLD, 1 HLL */
 static int g_scheme = 3;    /* 2 = live RK2 (Halfstep/Fullstep), 3 = RK3 */
 static int g_cooling = 0;   /* 0 off, 1 on */
 static int g_gravity = 0;   /* 0 off, 1 spiral+axisymmetric on */
 
-static int dispatch_lim_x(void) { return g_limiter ? MCLimiterX() : MinmodLimiterX(); }
-static int dispatch_lim_y(void) { return g_limiter ? MCLimiterY() : MinmodLimiterY(); }
-static int dispatch_lim_z(void) { return g_limiter ? MCLimiterZ() : MinmodLimiterZ(); }
+static int dispatch_lim_x(void)
+{
+	return g_limiter == 3 ? SuperbeeLimiterX() : g_limiter == 2 ? VanLeerLimiterX()
+	     : g_limiter ? MCLimiterX() : MinmodLimiterX();
+}
+static int dispatch_lim_y(void)
+{
+	return g_limiter == 3 ? SuperbeeLimiterY() : g_limiter == 2 ? VanLeerLimiterY()
+	     : g_limiter ? MCLimiterY() : MinmodLimiterY();
+}
+static int dispatch_lim_z(void)
+{
+	return g_limiter == 3 ? SuperbeeLimiterZ() : g_limiter == 2 ? VanLeerLimiterZ()
+	     : g_limiter ? MCLimiterZ() : MinmodLimiterZ();
+}
 static int dispatch_rs_x(void) { return g_solver ? HLLX() : HLLDX(); }
 static int dispatch_rs_y(void) { return g_solver ? HLLY() : HLLDY(); }
 static int dispatch_rs_z(void) { return g_solver ? HLLZ() : HLLDZ(); }

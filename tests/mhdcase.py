@@ -9,6 +9,10 @@ VARIANTS = {
     "rk3_mc_hlld_grav_cool": ("disc2", {}),
     "rk3_minmod_hll": ("disc1", {"solver": "hll"}),
     "rk2_mc_hll_grav_cool": ("disc2", {"scheme": 2, "solver": "hll"}),
+    "rk3_vanleer_hlld": ("disc1", {"limiter": "vanleer"}),
+    "rk2_vanleer_hlld_grav_cool": ("disc2", {"scheme": 2, "limiter": "vanleer"}),
+    "rk3_superbee_hll_grav_cool": ("disc2", {"solver": "hll", "limiter": "superbee"}),
+    "rk2_superbee_hlld": ("disc1", {"scheme": 2, "limiter": "superbee"}),
 }
 
 

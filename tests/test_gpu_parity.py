@@ -28,7 +28,8 @@ def describe(a, b):
     return "max|diff|=%g at %s (a=%r b=%r)" % (np.nanmax(d), idx, a[idx] if idx else None, b[idx] if idx else None)
 
 
-@pytest.mark.parametrize("variant", ["rk3_minmod_hlld", "rk3_mc_hlld_grav_cool", "rk3_minmod_hll"])
+@pytest.mark.parametrize("variant", ["rk3_minmod_hlld", "rk3_mc_hlld_grav_cool", "rk3_minmod_hll",
+                                     "rk3_vanleer_hlld", "rk3_superbee_hll_grav_cool"])
 @pytest.mark.parametrize("dims", [SMALL, ODD])
 def test_probes_bitwise(M, P, variant, dims):
     grid, params, U, V = make_case(M, variant, dims)
