@@ -194,7 +194,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     *out = NULL;
     int rc = check_grid(g);
     if (rc) return rc;
-    if (p->limiter < 0 || p->limiter > 3 || p->solver < 0 || p->solver > 1 ||
+    if (p->limiter < 0 || p->limiter > 3 || p->solver < 0 || p->solver > 1 || p->source < 0 || p->source > 3 ||
         (p->scheme != MHD_SCHEME_RK2 && p->scheme != MHD_SCHEME_RK3) || p->precision < 0 || p->precision > 1)
         return MHD_ERR_ARG;
     int ndev = 0;
@@ -330,6 +330,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     G.armnum = (double)p->armnum; G.cotpitch = cotpitch;
     G.cooling = p->cooling; G.gravity = p->gravity; G.limiter = p->limiter; G.solver = p->solver;
     G.scheme = p->scheme;
+    G.source = p->source;
     G.repair_irmax = ctx->fp32 ? 4 : 0;
 
     /* ---- state ---- */

@@ -19,6 +19,7 @@ MHD_ERR_ARG = -1
 MHD_ERR_DT = -3
 MHD_ERR_IO = -8
 LIMITER = {"minmod": 0, "mc": 1, "vanleer": 2, "superbee": 3}
+SOURCE = {"spiral": 0, "axi": 1, "uniformgz": 2, "none": 3}
 SOLVER = {"hlld": 0, "hll": 1}
 PREC = {"fp64": 0, "fp32": 1}
 
@@ -30,7 +31,7 @@ class MhdParams(C.Structure):
                 ("scalephase", C.c_double), ("armnum", C.c_int), ("omegasp", C.c_double),
                 ("omegapattern", C.c_double), ("pitch", C.c_double), ("limiter", C.c_int),
                 ("solver", C.c_int), ("scheme", C.c_int), ("cooling", C.c_int),
-                ("gravity", C.c_int), ("precision", C.c_int)]
+                ("gravity", C.c_int), ("precision", C.c_int), ("source", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -176,6 +177,8 @@ def default_params(**over):
             v = SOLVER[v]
         if k in ("precision",) and isinstance(v, str):
             v = PREC[v]
+        if k in ("source",) and isinstance(v, str):
+            v = SOURCE[v]
         setattr(p, k, v)
     return p
 

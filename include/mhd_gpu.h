@@ -50,6 +50,10 @@ extern "C" {
 #define MHD_SOLVER_HLL 1      /* HLLX/Y/Z (hllx.h:29, hlly.h:29, hllz.h:26) */
 #define MHD_SCHEME_RK2 2      /* live TVDRK: Halfstep + Fullstep (tvdrungekutta.h:31-41) */
 #define MHD_SCHEME_RK3 3      /* FirstStep/SecondStep/ThirdStep (tvdrungekutta.h:56-83) */
+#define MHD_SOURCE_SPIRAL 0   /* SpiralGravityCooling (source.h:26), the reference's choice */
+#define MHD_SOURCE_AXI 1      /* AxiGravityCooling / AxiGravity (source.h:143,207): cooling flag picks */
+#define MHD_SOURCE_UNIFORMGZ 2 /* UniformGz (source.h:269): g_z = -1, no geometric terms */
+#define MHD_SOURCE_NONE 3     /* NoSource (source.h:308): the geometric terms only */
 #define MHD_PREC_FP64 0       /* plain FP64: bit-identical to the reference C */
 #define MHD_PREC_FP32 1       /* FP32 state and fluxes, FP64 repair of the fragile steps */
 
@@ -66,6 +70,7 @@ typedef struct {
     int cooling;    /* 0 off, 1 Cooling() of cooling.h:22 */
     int gravity;    /* 0 off, 1 Gr*axi + SpiralGravity() each step */
     int precision;  /* MHD_PREC_* */
+    int source;     /* MHD_SOURCE_*: the source function the stages call */
 } mhd_params;
 
 /* Grid construction parameters (input.h:45-76). */

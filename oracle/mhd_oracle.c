@@ -971,13 +971,41 @@ static void riemann(orc_ctx *o, int dir, double *Fd)
 }
 
 /* ------------------------------------------------------------------------ */
-/* source.h:26-134 (SpiralGravityCooling)                                    */
+/* source.h:26-134 (SpiralGravityCooling); AxiGravityCooling (:143-204) and  */
+/* AxiGravity (:207-266) are its i < irin branch everywhere, with cooling on */
+/* or off; UniformGz (:269-305); NoSource (:308-349)                         */
 /* ------------------------------------------------------------------------ */
+static void source_other(orc_ctx *o)
+{
+    int i;
+#pragma omp parallel for
+    for (i = 0; i < o->ixmax; i++) {
+        double oxi = o->oneox[i];
+        for (int j = 0; j < o->jymax; j++)
+            for (int k = 0; k < o->kzmax; k++) {
+                size_t q = IDX(o, i, j, k), nc = o->nc;
+                const double *V = o->V;
+                double v0 = V[q], v1 = V[nc + q], v2 = V[2 * nc + q], v3 = V[3 * nc + q];
+                double v4 = V[4 * nc + q], v5 = V[5 * nc + q], v6 = V[6 * nc + q], v7 = V[7 * nc + q];
+                double *S = o->S;
+                for (int m = 0; m < 9; m++) S[m * nc + q] = 0.0;
+                if (o->p.source == 2) {
+                    S[3 * nc + q] = -v0 * 1.0;
+                    S[7 * nc + q] = -v3 * v0 * 1.0;
+                } else {
+                    S[nc + q] = (v0 * v2 * v2 - v5 * v5 + (v7 + 0.5 * (v4 * v4 + v5 * v5 + v6 * v6))) * oxi;
+                    S[5 * nc + q] = (v5 * v1 - v2 * v4) * oxi;
+                }
+            }
+    }
+}
+
 static void source(orc_ctx *o)
 {
     const orc_params *p = &o->p;
     double omegasp = p->omegasp;
     int i;
+    if (p->source >= 2) { source_other(o); return; }
 #pragma omp parallel for
     for (i = 0; i < o->ixmax; i++) {
         double xi = o->x[i], oxi = o->oneox[i];
@@ -990,7 +1018,7 @@ static void source(orc_ctx *o)
                 double *S = o->S;
                 int cl = cool(o, v0, v7);
                 S[q] = 0.0;
-                if (i < o->irin) {
+                if (i < o->irin || p->source == 1) {
                     double gx = o->graxi[q], gz = o->graxi[2 * nc + q];
                     S[nc + q] = ((v0 * v2 * v2 - v5 * v5 + (v7 + 0.5 * (v4 * v4 + v5 * v5 + v6 * v6))) * oxi
                                  + v0 * gx + v0 * omegasp * omegasp * xi + (2.0 * v0 * v2 * omegasp));

@@ -41,6 +41,7 @@ typedef struct {
     int scheme;    /* 2 live RK2 (halfstep/fullstep), 3 RK3 (first/second/thirdstep) */
     int cooling;   /* 0 off, 1 cooling.h:22 */
     int gravity;   /* 0 off, 1 axisymmetric + spiral (initialgravity.h, spiralgravity.h) */
+    int source;    /* 0 SpiralGravityCooling, 1 AxiGravity(Cooling), 2 UniformGz, 3 NoSource (source.h) */
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;

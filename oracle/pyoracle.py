@@ -24,7 +24,7 @@ GRIDSPEC_FIELDS = ["ix", "jy", "kz", "x0", "dx0", "lx", "y0", "ly", "z0", "dz0",
                    "stretchratio", "dxmax", "dzmax", "rin"]
 PARAM_FIELDS = ["cfl", "dtmin", "rhocr", "prcr", "betacr", "epssp0", "tausp", "scalez",
                 "scaler", "scalephase", "armnum", "omegasp", "omegapattern", "pitch"]
-FLAG_FIELDS = ["limiter", "solver", "scheme", "cooling", "gravity"]
+FLAG_FIELDS = ["limiter", "solver", "scheme", "cooling", "gravity", "source"]
 
 
 class _GridSpec(C.Structure):

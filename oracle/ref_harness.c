@@ -12,7 +12,8 @@
  *     (halfstep.h:163);
  *   - run-time variant selection by redirecting the names the stage functions
  *     call (halfstep.h:40-77, firststep.h:37-78): minmod, MC, van Leer or
- *     superbee limiter, HLLD or HLL solver;
+ *     superbee limiter, HLLD or HLL solver, and the source function
+ *     (halfstep.h:84-86, firststep.h:85-89);
  *   - a cooling on/off switch in front of Cooling() (cooling.h:22);
  *   - TVD-RK3 driven exactly as the commented block of tvdrungekutta.h:21,63-83
  *     (psi factor exp(-dt*ch/cr/3), then FirstStep, SecondStep, ThirdStep);
@@ -85,6 +86,7 @@ static int g_solver = 0;    /* 0 HLLD, 1 HLL */
 static int g_scheme = 3;    /* 2 = live RK2 (Halfstep/Fullstep), 3 = RK3 */
 static int g_cooling = 0;   /* 0 off, 1 on */
 static int g_gravity = 0;   /* 0 off, 1 spiral+axisymmetric on */
+static int g_source = 0;    /* 0 SpiralGravityCooling, 1 AxiGravity(Cooling), 2 UniformGz, 3 NoSource */
 
 static int dispatch_lim_x(void)
 {
@@ -105,6 +107,15 @@ static int dispatch_rs_x(void) { return g_solver ? HLLX() : HLLDX(); }
 static int dispatch_rs_y(void) { return g_solver ? HLLY() : HLLDY(); }
 static int dispatch_rs_z(void) { return g_solver ? HLLZ() : HLLDZ(); }
 
+static int dispatch_source(double dV[][ixmax][jymax][kzmax], double dS[][ixmax][jymax][kzmax])
+{
+	if (g_source == 1) return g_cooling ? AxiGravityCooling(dV, dS) : AxiGravity(dV, dS);
+	if (g_source == 2) return UniformGz(dV, dS);
+	if (g_source == 3) return NoSource(dV, dS);
+	return SpiralGravityCooling(dV, dS);
+}
+
+#define SpiralGravityCooling dispatch_source
 #define MinmodLimiterX dispatch_lim_x
 #define MinmodLimiterY dispatch_lim_y
 #define MinmodLimiterZ dispatch_lim_z
@@ -117,6 +128,7 @@ static int dispatch_rs_z(void) { return g_solver ? HLLZ() : HLLDZ(); }
 #include "secondstep.h"
 #include "thirdstep.h"
 #include "tvdrungekutta.h"
+#undef SpiralGravityCooling
 #undef MinmodLimiterX
 #undef MinmodLimiterY
 #undef MinmodLimiterZ
@@ -148,7 +160,7 @@ void ref_dims(int *out)
 
 /* params: 0 cfl, 1 dtmin, 2 rhocr, 3 prcr, 4 betacr, 5 epssp0, 6 tausp,
  * 7 scalez, 8 scaler, 9 scalephase, 10 armnum, 11 omegasp, 12 omegapattern,
- * 13 pitch; flags: limiter, solver, scheme, cooling, gravity. */
+ * 13 pitch; flags: limiter, solver, scheme, cooling, gravity, source. */
 void ref_set_params(const double *p, const int *flags)
 {
 	cfl = p[0]; dtmin = p[1]; rhocr = p[2]; prcr = p[3]; betacr = p[4];
@@ -156,7 +168,7 @@ void ref_set_params(const double *p, const int *flags)
 	scalephase = p[9]; armnum = (int)p[10]; omegasp = p[11];
 	omegapattern = p[12]; pitch = p[13];
 	g_limiter = flags[0]; g_solver = flags[1]; g_scheme = flags[2];
-	g_cooling = flags[3]; g_gravity = flags[4];
+	g_cooling = flags[3]; g_gravity = flags[4]; g_source = flags[5];
 }
 
 void ref_grid(void) { CylindricalGrid(); }

@@ -13,6 +13,10 @@ VARIANTS = {
     "rk2_vanleer_hlld_grav_cool": ("disc2", {"scheme": 2, "limiter": "vanleer"}),
     "rk3_superbee_hll_grav_cool": ("disc2", {"solver": "hll", "limiter": "superbee"}),
     "rk2_superbee_hlld": ("disc1", {"scheme": 2, "limiter": "superbee"}),
+    "rk3_minmod_hlld_axi_cool": ("disc2", {"limiter": "minmod", "source": "axi"}),
+    "rk2_minmod_hll_axi": ("disc2", {"scheme": 2, "solver": "hll", "cooling": 0, "source": "axi"}),
+    "rk2_mc_hlld_uniformgz": ("disc1", {"scheme": 2, "limiter": "mc", "source": "uniformgz"}),
+    "rk3_vanleer_hll_nosource": ("disc1", {"solver": "hll", "limiter": "vanleer", "source": "none"}),
 }
 
 
