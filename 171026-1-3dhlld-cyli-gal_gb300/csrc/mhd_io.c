@@ -8,6 +8,8 @@
  *                                            + mhd_check()
  *   SaveInitial()   saveinitial.h:18-50   -> mhd_save_initial()
  *   restart branch  main.c:244-272        -> mhd_restart()
+ *   GNUOutputCylinder() output.h:25-150   -> mhd_gnu_output_cylinder()
+ *   GDLOutputCylinder() output.h:280-390  -> mhd_gdl_output_cylinder()
  *
  * File format (one directory per output number, relative to a root
  * directory; the reference uses the working directory):
@@ -187,4 +189,113 @@ int mhd_restart(const char *root, int nout, double tint, const mhd_grid *g, cons
     if (t) *t = nout * tint;
     if (tout) *tout = (nout + 1) * tint;
     return MHD_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* text outputs for plotting                                                 */
+/* ------------------------------------------------------------------------ */
+static FILE *open_in(const char *root, const char *name)
+{
+    char path[4096];
+    if (snprintf(path, sizeof path, "%s/%s", root, name) >= (int)sizeof path) return NULL;
+    return fopen(path, "w");
+}
+
+/* one 1D cut: header, then x/y/z and rho vr vphi vz br bphi bz E p per cell */
+static int write_cut(const char *root, const char *name, int nstep, double t, int h1, int h2, const double *coord,
+                     size_t n, size_t q0, size_t stride, size_t nc, const double *U, const double *V)
+{
+    FILE *f = open_in(root, name);
+    if (!f) return MHD_ERR_IO;
+    int bad = fprintf(f, "#\t nstep=%d,\ttime=%.3e,\tj=%d,\tk=%d \n", nstep, t, h1, h2) < 0;
+    bad |= fprintf(f, "#%s rho vx vy vz bx by bz en pr\n", name[3] == 'r' ? "x" : name[3] == 'p' ? "y" : "z") < 0;
+    for (size_t c = 1; c + 1 < n && !bad; c++) {
+        size_t q = q0 + c * stride;
+        bad |= fprintf(f,
+                       "%.3e\t"
+                       "%.3e\t%.3e\t%.3e\t%.3e\t"
+                       "%.3e\t%.3e\t%.3e\t%.3e\t"
+                       "%.3e\n",
+                       coord[c], V[q], V[nc + q], V[2 * nc + q], V[3 * nc + q], V[4 * nc + q], V[5 * nc + q],
+                       V[6 * nc + q], U[7 * nc + q], V[7 * nc + q]) < 0;
+    }
+    bad |= fclose(f) != 0;
+    return bad ? MHD_ERR_IO : MHD_OK;
+}
+
+/* GNUOutputCylinder (output.h:25-150): 1d-r-<nout>.dat along r at j=1, k=1;
+ * 1d-phi-<nout>.dat along phi and 1d-z-<nout>.dat along z at the fixed
+ * radial index 160 (so the grid needs ix >= 159), with the header and column
+ * formats of the reference (E is the conserved total energy U[7]). */
+int mhd_gnu_output_cylinder(const char *root, int nout, int nstep, double t, const mhd_grid *g, const double *U,
+                            const double *V)
+{
+    if (!root || !g || !U || !V || nout < 0) return MHD_ERR_ARG;
+    const size_t ixmax = (size_t)g->ix + 2, jymax = (size_t)g->jy + 2, kzmax = (size_t)g->kz + 2;
+    const size_t nc = ixmax * jymax * kzmax;
+    const int icut = 160;
+    if (ixmax <= (size_t)icut + 1) return MHD_ERR_ARG;
+    char name[64];
+    int rc;
+    snprintf(name, sizeof name, "1d-r-%d.dat", nout);
+    if ((rc = write_cut(root, name, nstep, t, 1, 1, g->x, ixmax, 1 * kzmax + 1, jymax * kzmax, nc, U, V))) return rc;
+    snprintf(name, sizeof name, "1d-phi-%d.dat", nout);
+    if ((rc = write_cut(root, name, nstep, t, icut, 1, g->y, jymax, (size_t)icut * jymax * kzmax + 1, kzmax, nc, U,
+                        V)))
+        return rc;
+    snprintf(name, sizeof name, "1d-z-%d.dat", nout);
+    return write_cut(root, name, nstep, t, icut, 1, g->z, kzmax, ((size_t)icut * jymax + 1) * kzmax, 1, nc, U, V);
+}
+
+static int write_column(const char *root, const char *name, const double *a, size_t n)
+{
+    FILE *f = open_in(root, name);
+    if (!f) return MHD_ERR_IO;
+    int bad = 0;
+    for (size_t c = 1; c + 1 < n && !bad; c++) bad |= fprintf(f, "%e\n", a[c]) < 0;
+    bad |= fclose(f) != 0;
+    return bad ? MHD_ERR_IO : MHD_OK;
+}
+
+/* GDLOutputCylinder (output.h:280-390): r.dat, phi.dat, z.dat (interior
+ * centres), the k=1 slices 2d-density-rphi, 2d-pressure-rphi,
+ * 2d-benergy-rphi (B^2/2) with j fastest, and the j=0 slice 2d-density-rz
+ * with r fastest; one "%e" value per line. */
+int mhd_gdl_output_cylinder(const char *root, int nout, const mhd_grid *g, const double *V)
+{
+    if (!root || !g || !V || nout < 0) return MHD_ERR_ARG;
+    const size_t ixmax = (size_t)g->ix + 2, jymax = (size_t)g->jy + 2, kzmax = (size_t)g->kz + 2;
+    const size_t nc = ixmax * jymax * kzmax;
+    int rc;
+    if ((rc = write_column(root, "r.dat", g->x, ixmax))) return rc;
+    if ((rc = write_column(root, "phi.dat", g->y, jymax))) return rc;
+    if ((rc = write_column(root, "z.dat", g->z, kzmax))) return rc;
+    static const char *const slice[3] = {"2d-density-rphi", "2d-pressure-rphi", "2d-benergy-rphi"};
+    for (int s = 0; s < 3; s++) {
+        char name[64];
+        snprintf(name, sizeof name, "%s-%d.dat", slice[s], nout);
+        FILE *f = open_in(root, name);
+        if (!f) return MHD_ERR_IO;
+        int bad = 0;
+        for (size_t i = 1; i + 1 < ixmax && !bad; i++)
+            for (size_t j = 1; j + 1 < jymax && !bad; j++) {
+                size_t q = (i * jymax + j) * kzmax + 1;
+                double v = s == 0 ? V[q]
+                         : s == 1 ? V[7 * nc + q]
+                                  : 0.5 * (V[4 * nc + q] * V[4 * nc + q] + V[5 * nc + q] * V[5 * nc + q]
+                                           + V[6 * nc + q] * V[6 * nc + q]);
+                bad |= fprintf(f, "%e\n", v) < 0;
+            }
+        bad |= fclose(f) != 0;
+        if (bad) return MHD_ERR_IO;
+    }
+    char name[64];
+    snprintf(name, sizeof name, "2d-density-rz-%d.dat", nout);
+    FILE *f = open_in(root, name);
+    if (!f) return MHD_ERR_IO;
+    int bad = 0;
+    for (size_t k = 1; k + 1 < kzmax && !bad; k++)
+        for (size_t i = 1; i + 1 < ixmax && !bad; i++) bad |= fprintf(f, "%e\n", V[(i * jymax + 0) * kzmax + k]) < 0;
+    bad |= fclose(f) != 0;
+    return bad ? MHD_ERR_IO : MHD_OK;
 }

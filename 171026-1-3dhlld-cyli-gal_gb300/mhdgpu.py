@@ -100,6 +100,9 @@ def lib():
         "mhd_save_initial": (C.c_int, [C.POINTER(MhdGrid), C.c_double, DP, DP, vp, vp, vp]),
         "mhd_restart": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.POINTER(MhdGrid), C.POINTER(MhdParams),
                                   DP, DP, DP, DP, DP, _PD, _PD]),
+        "mhd_gnu_output_cylinder": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.POINTER(MhdGrid),
+                                              DP, DP]),
+        "mhd_gdl_output_cylinder": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(MhdGrid), DP]),
         "mhd_checkpoint_begin": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_double]),
         "mhd_checkpoint_wait": (C.c_int, [vp]),
         "mhd_create": (C.c_int, [C.POINTER(MhdGrid), C.POINTER(MhdParams), C.POINTER(vp)]),
@@ -315,6 +318,15 @@ def binary_output(root, nout, t, grid, V):
     """BinaryOutput() of V into <root>/<nout>/ (mhd_binary_output)."""
     V = np.ascontiguousarray(V, dtype=np.float64)
     check(lib().mhd_binary_output(_path(root), int(nout), float(t), C.byref(grid.g), V), "mhd_binary_output")
+
+
+def text_output(root, nout, nstep, t, grid, U, V):
+    """GNUOutputCylinder + GDLOutputCylinder files under root."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    check(lib().mhd_gnu_output_cylinder(_path(root), int(nout), int(nstep), float(t), C.byref(grid.g), U, V),
+          "mhd_gnu_output_cylinder")
+    check(lib().mhd_gdl_output_cylinder(_path(root), int(nout), C.byref(grid.g), V), "mhd_gdl_output_cylinder")
 
 
 def restart_read(root, num, grid):

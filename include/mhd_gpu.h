@@ -174,6 +174,17 @@ int mhd_save_initial(const mhd_grid *g, double rhocr, const double *U, const dou
 int mhd_restart(const char *root, int nout, double tint, const mhd_grid *g, const mhd_params *p, double *U,
                 double *V, double *Uinit, double *Vinit, double *rhofloor, double *t, double *tout);
 
+/* Text outputs for plotting, the reference's formats, written under root:
+ * GNUOutputCylinder (output.h:25-150): 1d-r-<nout>.dat (j=1, k=1),
+ * 1d-phi-<nout>.dat and 1d-z-<nout>.dat at the radial index 160 the
+ * reference fixes (MHD_ERR_ARG when ix < 159); columns coordinate, rho, v_r,
+ * v_phi, v_z, B_r, B_phi, B_z, E (= U[7]), p.  GDLOutputCylinder
+ * (output.h:280-390): r.dat, phi.dat, z.dat, the k=1 slices
+ * 2d-{density,pressure,benergy}-rphi-<nout>.dat and 2d-density-rz-<nout>.dat. */
+int mhd_gnu_output_cylinder(const char *root, int nout, int nstep, double t, const mhd_grid *g, const double *U,
+                            const double *V);
+int mhd_gdl_output_cylinder(const char *root, int nout, const mhd_grid *g, const double *V);
+
 /* ---- device context: the step ------------------------------------------- */
 int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out);
 void mhd_destroy(mhd_ctx *ctx);

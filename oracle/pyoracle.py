@@ -264,6 +264,7 @@ class RefOracle(_Common):
         lib.ref_set_threads(1)
         lib.ref_binary_output.argtypes = [C.c_int, C.c_double]
         lib.ref_restart_read.argtypes = [C.c_int]
+        lib.ref_text_output.argtypes = [C.c_int, C.c_int, C.c_double]
         lib.ref_check_flags.argtypes = [_IP]
         self.lib = lib
         self.rhocr = float(params["rhocr"])
@@ -292,6 +293,10 @@ class RefOracle(_Common):
     def binary_output(self, num, t):
         """BinaryOutput() into ./<num>/ of the current working directory."""
         self.lib.ref_binary_output(int(num), float(t))
+
+    def text_output(self, num, nstep, t):
+        """GNUOutputCylinder() + GDLOutputCylinder() into the working directory."""
+        self.lib.ref_text_output(int(num), int(nstep), float(t))
 
     def restart_read(self, num):
         """RestartRead(num) from ./<num>/: V from the files, VtoU, Check;

@@ -353,6 +353,15 @@ void ref_binary_output(int num, double tnow)
 	BinaryOutput();
 }
 
+/* GNUOutputCylinder() and GDLOutputCylinder() (output.h:25-390) into the
+ * working directory */
+void ref_text_output(int num, int step, double tnow)
+{
+	nout = num; nstep = step; t = tnow;
+	GNUOutputCylinder();
+	GDLOutputCylinder();
+}
+
 /* RestartRead(num) (restartread.h:9-143): V from ./<num>/, VtoU, Check */
 void ref_restart_read(int num) { RestartRead(num); }
 

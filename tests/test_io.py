@@ -133,3 +133,28 @@ def test_restart_errors(M, tmp_path):
     x = grid.arr("x", grid.ixmax)
     assert M.lib().mhd_binary_output_arrays(b"x", -1, 0.0, 12, 8, 12, x, x, x, V) == M.MHD_ERR_ARG
     assert M.lib().mhd_restart_read(str(tmp_path).encode(), 1, 0, 8, 12, V) == M.MHD_ERR_ARG
+
+
+@needs_ref
+def test_text_outputs_match_reference(M, P, tmp_path):
+    """GNUOutputCylinder / GDLOutputCylinder: the same files, byte for byte, on
+    the shipped grid family (the reference cuts at radial index 160)."""
+    from mhdcase import make_shipped
+    grid, params, U, V, Ui, Vi, rf = make_shipped(M, (220, 8, 120))
+    r = P.RefOracle(grid.ix, grid.jy, grid.kz, M.oracle_params(params), shipped=True)
+    r.galactic_disc3()
+    Ur, Vr, _ = r.store()
+    a, b = tmp_path / "ref", tmp_path / "lib"
+    a.mkdir()
+    b.mkdir()
+    with chdir(a):
+        r.text_output(5, 1234, 0.25)
+    M.text_output(b, 5, 1234, 0.25, grid, Ur, Vr)
+    names = sorted(p.name for p in a.iterdir())
+    assert names == sorted(p.name for p in b.iterdir()) and len(names) == 10
+    for name in names:
+        assert (a / name).read_bytes() == (b / name).read_bytes(), name
+    small, params2, U2, V2 = make_case(M, "rk3_minmod_hlld", (64, 8, 12))
+    with pytest.raises(M.MhdError) as e:
+        M.text_output(b, 1, 0, 0.0, small, U2, V2)      # no radial index 160 on this grid
+    assert e.value.code == M.MHD_ERR_ARG
