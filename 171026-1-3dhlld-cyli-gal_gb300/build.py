@@ -20,6 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libmhdgpu.so")
+HOSTEXE = os.path.join(LIBDIR, "mhd_disc")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -73,14 +74,20 @@ def build(force=False, verbose=False):
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = _sources()
     newest = max(os.path.getmtime(p) for p in [os.path.join(CSRC, s) for s in srcs] + _headers())
-    newest = max(newest, os.path.getmtime(__file__))
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+    newest = max(newest, os.path.getmtime(__file__), os.path.getmtime(os.path.join(PKG, "host", "mhd_disc_main.c")))
+    if (not force and os.path.exists(LIB) and os.path.exists(HOSTEXE)
+            and min(os.path.getmtime(LIB), os.path.getmtime(HOSTEXE)) >= newest):
         return LIB
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(_compile, srcs))
     cmd = ["nvcc"] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lm"]
     subprocess.check_call(cmd)
     os.replace(LIB + ".tmp", LIB)
+    # the C host program (the reference's main.c on the C-ABI), next to the library
+    subprocess.check_call(["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-I", INCLUDE,
+                           os.path.join(PKG, "host", "mhd_disc_main.c"), "-o", HOSTEXE + ".tmp",
+                           "-L", LIBDIR, "-lmhdgpu", "-Wl,-rpath,$ORIGIN"])
+    os.replace(HOSTEXE + ".tmp", HOSTEXE)
     if verbose:
         for s in srcs:
             print(open(os.path.join(OBJ, s + ".log")).read())
