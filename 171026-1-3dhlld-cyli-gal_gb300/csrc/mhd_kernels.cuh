@@ -211,7 +211,7 @@ __device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a,
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) update_kernel(Geom G, StageArgs<T> a)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1) update_kernel(Geom G, StageArgs<T> a)
 {
     if (a.sc->dtbad) return;
     const int k = 1 + blockIdx.x * blockDim.x + threadIdx.x;

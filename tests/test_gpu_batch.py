@@ -46,7 +46,12 @@ def test_batch_matches_single_disc_runs(M):
         Us, _ = s.download()
         Ub, _ = b.download(d)
         assert abs(ts - t[d]) <= 1e-12 * ts, d
-        assert np.all(rel_l1(Ub[:8], Us[:8]) <= 1e-6), (d, rel_l1(Ub, Us))
+        err = rel_l1(Ub[:8], Us[:8])
+        # B_r, B_z start at zero in these discs: against the field scale
+        bscale = np.abs(Us[4:7]).sum()
+        for m in (4, 6):
+            err[m] = np.abs(Ub[m] - Us[m]).sum() / bscale
+        assert np.all(err <= 1e-6), (d, err)
         s.close()
     b.close()
 
