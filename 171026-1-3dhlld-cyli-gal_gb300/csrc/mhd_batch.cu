@@ -34,6 +34,7 @@
 #include <string.h>
 
 #include <new>
+#include <algorithm>
 #include <vector>
 
 #include "mhd_ctx_internal.h"
@@ -394,6 +395,11 @@ struct mhd_batch {
     uint2 *dtiles, *ddt;
     int ntiles, ndt_tiles, rows_per_tile;
     int phased;                 /* 1: one launch per phase, 0: one persistent launch per stage */
+    int discgraph;              /* 1: every disc's own device-resident step, all in one graph */
+    int nbranch;                /*    on this many parallel stream branches */
+    std::vector<cudaStream_t> bst;
+    std::vector<cudaEvent_t> bev;
+    long long step_launches;    /* kernels per step of the captured graph */
     uint4 *dph[4];              /* phased row tiles: flux r, phi, z, update */
     int nph[4];
     uint2 *dghost;
@@ -491,9 +497,50 @@ static cudaError_t launch_stage(mhd_batch *b, int *head, int *done, int kind, in
 }
 
 /* the launches of one step of all discs, starting at primitive parity `parity` */
+/* disc-graph mode: fork from the batch stream into nbranch streams, each
+ * running its share of the discs' single-disc steps one after another (discs
+ * dealt largest first to the least-loaded branch), then join */
+static int enqueue_disc_graph(mhd_batch *b, int parity)
+{
+    const int n = b->n, K = b->nbranch;
+    while ((int)b->bst.size() < K + 1) {
+        cudaStream_t s;
+        cudaEvent_t e;
+        BCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        b->bst.push_back(s);
+        BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->bev.push_back(e);
+    }
+    std::vector<int> order(n);
+    for (int d = 0; d < n; d++) order[d] = d;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return b->ctx[x]->nc > b->ctx[y]->nc; });
+    std::vector<long long> load(K, 0);
+    std::vector<std::vector<int>> part(K);
+    for (int d : order) {
+        int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        part[k].push_back(d);
+        load[k] += b->ctx[d]->nc;
+    }
+    BCK(cudaEventRecord(b->bev[K], b->st));
+    long long launches = 0;
+    for (int k = 0; k < K; k++) {
+        BCK(cudaStreamWaitEvent(b->bst[k], b->bev[K], 0));
+        for (int d : part[k]) {
+            b->ctx[d]->vcur = parity;
+            int rc = mhd_ctx_enqueue_step(b->ctx[d], b->bst[k], &launches);
+            if (rc) return rc;
+        }
+        BCK(cudaEventRecord(b->bev[k], b->bst[k]));
+        BCK(cudaStreamWaitEvent(b->st, b->bev[k], 0));
+    }
+    b->step_launches = launches;
+    return MHD_OK;
+}
+
 static int enqueue_batch_step(mhd_batch *b, int parity)
 {
     const int n = b->n;
+    if (b->discgraph) return enqueue_disc_graph(b, parity);
     BCK(cudaMemsetAsync(b->dcnt, 0, 9 * n * sizeof(int), b->st));
     batch_setdt_kernel<<<b->ndt_tiles, 256, 0, b->st>>>(b->dd, parity ? b->ddt + b->ndt_tiles : b->ddt,
                                                          b->rows_per_tile);
@@ -666,6 +713,13 @@ extern "C" int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *
     }
     b->persistent = fp32;
     if (fp32) {
+        for (int i = 0; i < n; i++) {
+            int rc = mhd_ctx_prepare_run(b->ctx[i]);
+            if (rc) {
+                mhd_batch_destroy(b);
+                return rc;
+            }
+        }
         int rc = setup_persistent(b);
         if (rc) {
             mhd_batch_destroy(b);
@@ -686,6 +740,8 @@ extern "C" void mhd_batch_destroy(mhd_batch *b)
                  b->dph[3], b->dghost};
     for (size_t q = 0; q < sizeof p / sizeof p[0]; q++)
         if (p[q]) cudaFree(p[q]);
+    for (cudaStream_t s2 : b->bst) { cudaStreamSynchronize(s2); cudaStreamDestroy(s2); }
+    for (cudaEvent_t e : b->bev) cudaEventDestroy(e);
     if (b->st) cudaStreamDestroy(b->st);
     for (mhd_ctx *c : b->ctx)
         if (c) mhd_destroy(c);
@@ -730,7 +786,7 @@ static int batch_run(mhd_batch *b, int nsteps, double *t, int *status)
         int rc = build_graphs(b);
         if (rc) return rc;
     }
-    long long per_step = 3 + b->nst * (b->phased ? 5 : 1) + 1;
+    long long per_step = b->discgraph ? b->step_launches : 3 + b->nst * (b->phased ? 5 : 1) + 1;
     for (int s = 0; s < nsteps; s++) {
         BCK(cudaGraphLaunch(b->gx[b->parity], b->st));
         b->parity ^= (b->nst & 1);
@@ -766,6 +822,28 @@ extern "C" int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status)
         }
     if (status)
         for (int i = 0; i < b->n; i++) status[i] = b->stopped[i] ? MHD_ERR_DT : MHD_OK;
+    return MHD_OK;
+}
+
+extern "C" int mhd_batch_set_mode(mhd_batch *b, int mode, int arg)
+{
+    if (!b) return MHD_ERR_ARG;
+    if (!b->persistent) return mode == 0 ? MHD_OK : MHD_ERR_ARG;   /* plain form: per-disc mhd_step */
+    if (mode == 0) {
+        if (arg < 0 || arg >= NCAND) return MHD_ERR_ARG;
+        int rc = build_tiles(b, CANDIDATES[arg]);
+        if (rc) return rc;
+        b->nblk_stage = stage_blocks(b->cfg);
+    } else if (mode == 2) {
+        if (arg < 1 || arg > 64) return MHD_ERR_ARG;
+        b->nbranch = std::min(arg, b->n);
+    } else if (mode != 1) {
+        return MHD_ERR_ARG;
+    }
+    if (b->st) BCK(cudaStreamSynchronize(b->st));
+    b->phased = mode == 1;
+    b->discgraph = mode == 2;
+    b->graph_ready = 0;
     return MHD_OK;
 }
 
@@ -806,14 +884,25 @@ extern "C" int mhd_batch_tune(mhd_batch *b, int *best)
     BCK(cudaEventCreate(&e1));
     float best_ms = 1e30f;
     int best_i = 0;
-    for (int ci = 0; ci <= NCAND; ci++) {   /* NCAND = the phased mode */
-        int rc = restore();
-        if (rc) return rc;
+    /* candidates: the persistent tile shapes, then the phased mode, then the
+     * disc graph on 2, 4, 8 or 16 branches */
+    static const int BRANCHES[] = {2, 4, 8, 16};
+    const int nall = NCAND + 1 + 4;
+    auto select = [&](int ci) -> int {
         b->phased = ci == NCAND;
-        if (!b->phased) {
-            if ((rc = build_tiles(b, CANDIDATES[ci]))) return rc;
+        b->discgraph = ci > NCAND;
+        if (b->discgraph) b->nbranch = std::min(BRANCHES[ci - NCAND - 1], n);
+        if (ci < NCAND) {
+            int rc = build_tiles(b, CANDIDATES[ci]);
+            if (rc) return rc;
             b->nblk_stage = stage_blocks(b->cfg);
         }
+        return MHD_OK;
+    };
+    for (int ci = 0; ci < nall; ci++) {
+        int rc = restore();
+        if (rc) return rc;
+        if ((rc = select(ci))) return rc;
         b->graph_ready = 0;
         tt = t0;
         if ((rc = batch_run(b, 1, tt.data(), NULL))) return rc;   /* warm-up + graph build */
@@ -830,14 +919,12 @@ extern "C" int mhd_batch_tune(mhd_batch *b, int *best)
     int rc = restore();
     if (rc) return rc;
     for (int d = 0; d < n; d++) b->ctx[d]->h_sc->t = t0[d];
-    b->phased = best_i == NCAND;
-    if (!b->phased) {
-        if ((rc = build_tiles(b, CANDIDATES[best_i]))) return rc;
-        b->nblk_stage = stage_blocks(b->cfg);
-    }
+    if ((rc = select(best_i))) return rc;
     b->graph_ready = 0;
     (void)par0;
-    if (b->phased) {
+    if (b->discgraph) {
+        best[0] = b->nbranch; best[1] = 0; best[2] = 0; best[3] = 0; best[4] = 2;
+    } else if (b->phased) {
         best[0] = 1; best[1] = 1; best[2] = 128; best[3] = 128; best[4] = 1;
     } else {
         best[0] = CANDIDATES[best_i].ti;

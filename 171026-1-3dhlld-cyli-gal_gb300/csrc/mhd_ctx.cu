@@ -794,6 +794,31 @@ static int enqueue_device_step(mhd_ctx *ctx)
     return MHD_OK;
 }
 
+/* for the batched form: one device-resident step of ctx enqueued on stream s
+ * (captured with the other discs' into one graph); launches counts the
+ * kernels.  mhd_ctx_prepare_run() first, outside any capture. */
+int mhd_ctx_prepare_run(mhd_ctx *ctx)
+{
+    if (!ctx->d_cnt_run) CK(cudaMalloc((void **)&ctx->d_cnt_run, 9 * sizeof(int)));
+    return MHD_OK;
+}
+
+int mhd_ctx_enqueue_step(mhd_ctx *ctx, cudaStream_t s, long long *launches)
+{
+    if (!ctx->d_cnt_run || !ctx->fp32) return MHD_ERR_STATE;
+    cudaStream_t st0 = ctx->st;
+    int prof = ctx->prof;
+    long long l0 = ctx->launches;
+    ctx->st = s;
+    ctx->prof = 0;
+    int rc = enqueue_device_step(ctx);
+    ctx->st = st0;
+    ctx->prof = prof;
+    if (launches) *launches += ctx->launches - l0;
+    ctx->launches = l0;
+    return rc;
+}
+
 extern "C" int mhd_run(mhd_ctx *ctx, int nsteps, double *t)
 {
     if (!ctx || !t || nsteps < 0) return MHD_ERR_ARG;

@@ -62,4 +62,9 @@ struct mhd_ctx {
     int ck_pending, ck_status;
 };
 
+/* batched form: one device-resident step of a context on a given stream
+ * (mhd_ctx.cu) */
+int mhd_ctx_prepare_run(mhd_ctx *ctx);
+int mhd_ctx_enqueue_step(mhd_ctx *ctx, cudaStream_t s, long long *launches);
+
 #endif

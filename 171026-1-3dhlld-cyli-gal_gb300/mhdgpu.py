@@ -127,6 +127,7 @@ def lib():
         "mhd_batch_download": (C.c_int, [vp, C.c_int, vp, vp]),
         "mhd_batch_step": (C.c_int, [vp, C.c_int, DP, IP]),
         "mhd_batch_tune": (C.c_int, [vp, IP]),
+        "mhd_batch_set_mode": (C.c_int, [vp, C.c_int, C.c_int]),
         "mhd_upload_state": (C.c_int, [vp, vp, vp]),
         "mhd_prof_enable": (C.c_int, [vp, C.c_int]),
         "mhd_set_stage_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
@@ -539,6 +540,10 @@ class Batch:
         best = np.zeros(5, dtype=np.int32)
         check(lib().mhd_batch_tune(self.h, best), "mhd_batch_tune")
         return tuple(int(v) for v in best)
+
+    def set_mode(self, mode, arg=0):
+        """0 persistent (tile candidate arg), 1 phased, 2 disc graph on arg branches."""
+        check(lib().mhd_batch_set_mode(self.h, int(mode), int(arg)), "mhd_batch_set_mode")
 
 
 def batch_workload(n=64, seed=7):

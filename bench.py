@@ -184,7 +184,11 @@ def precision_report(args):
     """FP32 + FP64-repair form against the plain FP64 form (bit-identical to the
     reference C, checked on smaller grids by the tests) after N steps from the
     same state: per conserved variable relative L1 and Linf, and the drift of
-    the totals and max|div B| of both forms."""
+    the totals and max|div B| of both forms.  The same comparison for a plain
+    FP64 run started from the FP32-rounded state (fp64_twin) gives the floor:
+    the part of the difference a rounding-sized perturbation of the start
+    produces by itself.  m_r, m_z (against sum |rho v_phi|) and B_r, B_z, psi
+    (against sum |B|) are also reported relative to the flow's scales."""
     M = load_product()
     dims = tuple(int(v) for v in args.size.split("x")) if args.size else (256, 256, 128)
     (nr, nphi, nz), params, ic = M.workload(args.workload, nr=dims[0], nphi=dims[1], nz=dims[2],
@@ -196,9 +200,16 @@ def precision_report(args):
     out = {"report": "precision", "workload": args.workload, "dims": dims, "steps": args.precision_report,
            "solver": "hll" if params.solver == 1 else "hlld"}
     res = {}
-    for prec in ("fp64", "fp32"):
-        d = M.Disc(grid, with_precision(M, params, prec))
-        d.upload(U, V)
+    # fp64_twin: the plain form from the initial state rounded to FP32 -- how far
+    # a rounding-sized perturbation of the start alone carries in N steps
+    U32 = U.astype(np.float32).astype(np.float64)
+    V32 = V.astype(np.float32).astype(np.float64)
+    for prec in ("fp64", "fp32", "fp64_twin"):
+        d = M.Disc(grid, with_precision(M, params, "fp64" if prec == "fp64_twin" else prec))
+        if prec == "fp64_twin":
+            d.upload(U32, V32)
+        else:
+            d.upload(U, V)
         d0 = d.diagnostics()
         t = 0.0
         w0 = time.perf_counter()
@@ -220,15 +231,29 @@ def precision_report(args):
         out[prec] = {"t": t, "wall_s": wall,
                      "drift": {k: (d1[k] - d0[k]) / abs(d0[k]) if d0[k] else d1[k] for k in ("mass", "angmom", "energy")},
                      "maxdivb_end": d1["maxdivb"], "maxdivb_max": maxdivb, "psi_total_max": psi_max}
-    a, b = res["fp32"], res["fp64"]
     names = ["rho", "m_r", "r*m_phi", "m_z", "B_r", "B_phi", "B_z", "E", "psi"]
-    rl1, linf = {}, {}
-    for m in range(9):
-        den = np.abs(b[m]).sum()
-        rl1[names[m]] = float(np.abs(a[m] - b[m]).sum() / den) if den > 0 else float(np.abs(a[m] - b[m]).sum())
-        sc = np.abs(b[m]).max()
-        linf[names[m]] = float(np.abs(a[m] - b[m]).max() / sc) if sc > 0 else float(np.abs(a[m] - b[m]).max())
-    out["fp32_vs_fp64"] = {"rel_l1": rl1, "rel_linf": linf}
+    b = res["fp64"]
+    x = grid.arr("x", grid.ixmax)[:, None, None]
+    mscale = np.abs(b[2] / x).sum()          # sum |rho v_phi|: the momentum scale
+    bscale = np.abs(b[4:7]).sum()            # sum |B|: the field scale
+
+    def compare(a):
+        rl1, linf, scaled = {}, {}, {}
+        for m in range(9):
+            diff = np.abs(a[m] - b[m])
+            den = np.abs(b[m]).sum()
+            rl1[names[m]] = float(diff.sum() / den) if den > 0 else float(diff.sum())
+            sc = np.abs(b[m]).max()
+            linf[names[m]] = float(diff.max() / sc) if sc > 0 else float(diff.max())
+            # components that start at (or near) zero, against the flow's scales
+            if m in (1, 3):
+                scaled[names[m]] = float(diff.sum() / mscale)
+            elif m in (4, 6, 8):
+                scaled[names[m]] = float(diff.sum() / bscale)
+        return {"rel_l1": rl1, "rel_linf": linf, "rel_l1_of_scale": scaled}
+
+    out["fp32_vs_fp64"] = compare(res["fp32"])
+    out["fp64_twin_vs_fp64"] = compare(res["fp64_twin"])
     print(json.dumps(out))
     return 0
 
@@ -284,8 +309,9 @@ def batch_bench(args):
            "discs": n, "zones": zones, "steps": args.steps, "warmup": args.warmup,
            "value": zones * args.steps / wall, "unit": "zone-updates/s", "ms_per_step": wall / args.steps * 1e3,
            "sequential_single_disc": {"value": zones * args.steps / seq_wall, "ms_per_step": seq_wall / args.steps * 1e3},
-           "tuned": {"tile_r": best[0], "tile_phi": best[1], "tile_z": best[2], "threads": best[3],
-                     "mode": "phased" if best[4] else "persistent", "tune_seconds": tune_s},
+           "tuned": ({"mode": "disc_graph", "branches": best[0], "tune_seconds": tune_s} if best[4] == 2 else
+                     {"tile_r": best[0], "tile_phi": best[1], "tile_z": best[2], "threads": best[3],
+                      "mode": "phased" if best[4] == 1 else "persistent", "tune_seconds": tune_s}),
            "discs_stopped_by_dt_guard": stopped, "clocks": clocks,
            "sizes": [list(dims) for dims, _, _ in wl]}
     if args.batch_check:

@@ -276,15 +276,22 @@ int mhd_batch_upload(mhd_batch *b, int disc, const double *U, const double *V,
 int mhd_batch_download(mhd_batch *b, int disc, double *U, double *V);
 /* nsteps steps of every disc, each with its own dt; t[n] advance in place;
  * status[n] = 0 or MHD_ERR_DT for a disc whose dt guard fired (that disc then
- * stops advancing).  One persistent launch per RK stage, the whole step
- * captured as a CUDA graph. */
+ * stops advancing).  The whole step is one CUDA graph launch.  Precision form:
+ * by default one persistent launch per RK stage over a tile queue of all
+ * discs; mhd_batch_tune() may pick the phased or disc-graph mode instead.
+ * Plain form: the discs' mhd_step() one after another. */
 int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status);
 /* Times candidate configurations on the current state and keeps the fastest;
  * the state is restored afterwards.  Candidates: the persistent per-stage
- * launch with each compiled tile shape / block size / register cap, and the
- * phased form (one launch per stage phase over all discs).
- * best[5] = {tile_i, tile_j, tile_k, threads, phased}. */
+ * launch with each compiled tile shape / block size / register cap (mode 0),
+ * the phased form -- one launch per stage phase over all discs (mode 1) --
+ * and the disc graph -- every disc's own single-disc step, the discs dealt to
+ * 2, 4, 8 or 16 parallel stream branches of one graph (mode 2).
+ * best[5] = {tile_i, tile_j, tile_k, threads, mode}; mode 2: {branches, 0, 0, 0, 2}. */
 int mhd_batch_tune(mhd_batch *b, int *best);
+/* Pick the precision form's batch mode directly: 0 persistent with compiled
+ * tile candidate arg, 1 phased, 2 disc graph on arg branches (1..64). */
+int mhd_batch_set_mode(mhd_batch *b, int mode, int arg);
 
 /* ---- allocation-free CFL reduction -------------------------------------- */
 /* No counterpart in the reference.  For callers that may not call cudaMalloc
