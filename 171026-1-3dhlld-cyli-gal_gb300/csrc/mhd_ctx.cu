@@ -327,6 +327,9 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     G.spC1f = Fd + o_C1; G.spC2f = Fd + o_C2; G.spDf = Fd + o_D; G.zf = Fd + o_z;
     G.armnumf = (float)p->armnum; G.cotpitchf = (float)cotpitch;
     G.omegasp = p->omegasp; G.prcr = p->prcr; G.betacr = p->betacr; G.rhocr = p->rhocr;
+    G.oneobetacr = 1.0 / p->betacr;
+    G.omegaspf = (float)p->omegasp; G.prcrf = (float)p->prcr; G.betacrf = (float)p->betacr;
+    G.oneobetacrf = (float)(1.0 / p->betacr);
     G.armnum = (double)p->armnum; G.cotpitch = cotpitch;
     G.cooling = p->cooling; G.gravity = p->gravity; G.limiter = p->limiter; G.solver = p->solver;
     G.scheme = p->scheme;
