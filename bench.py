@@ -258,6 +258,52 @@ def precision_report(args):
     return 0
 
 
+def monitor_run(args):
+    """A long run with both Riemann solvers (and, on request, both forms):
+    max|div B|, sum|psi| dV and the conservation totals (FP64 diagnostics on the
+    device) every args.monitor_every steps, and the device time per step.  The
+    precision form runs mhd_run (device-resident dt, one graph per step)
+    between diagnostics; the plain form runs mhd_step."""
+    M = load_product()
+    dims = tuple(int(v) for v in args.size.split("x")) if args.size else (512, 512, 256)
+    out = {"report": "monitor", "workload": args.workload, "dims": dims, "steps": args.monitor}
+    runs = [(s_, p_) for p_ in args.monitor_forms.split(",") for s_ in args.monitor_solvers.split(",")]
+    for solver, prec in runs:
+        (nr, nphi, nz), params, ic = M.workload(args.workload, nr=dims[0], nphi=dims[1], nz=dims[2], solver=solver,
+                                                 precision=prec)
+        grid = M.Grid.disc(nr, nphi, nz)
+        if params.gravity:
+            grid.set_initial_gravity()
+        U, V = grid.ic_disc(**ic)
+        d = M.Disc(grid, params)
+        d.upload(U, V)
+        d0 = d.diagnostics()
+        rows = [{"step": 0, "t": 0.0, "maxdivb": d0["maxdivb"], "psi": d0["psi"], "mass": d0["mass"],
+                 "angmom": d0["angmom"], "energy": d0["energy"]}]
+        t, done, dev_ms = 0.0, 0, 0.0
+        while done < args.monitor:
+            n = min(args.monitor_every, args.monitor - done)
+            d.timer_start()
+            if prec == "fp32":
+                t = d.run(n, t)
+            else:
+                for _ in range(n):       # the plain form steps with host exp/sincos
+                    rc, t, *_ = d.step(t)
+                    if rc != 0:
+                        raise RuntimeError("dt guard fired")
+            dev_ms += d.timer_stop()
+            done += n
+            dg = d.diagnostics()
+            rows.append({"step": done, "t": t, "maxdivb": dg["maxdivb"], "psi": dg["psi"], "mass": dg["mass"],
+                         "angmom": dg["angmom"], "energy": dg["energy"]})
+        d.close()
+        zones = nr * nphi * nz
+        out[solver + "_" + prec] = {"ms_per_step": dev_ms / args.monitor,
+                                    "zone_updates_per_s": zones * args.monitor / (dev_ms / 1e3), "rows": rows}
+    print(json.dumps(out))
+    return 0
+
+
 def batch_bench(args):
     """Batched workload: 64 uneven discs (sizes from seed 7), precision form.
     value = all zones of all discs x steps / device time of the persistent
@@ -370,10 +416,17 @@ def main():
     ap.add_argument("--precision-report", type=int, default=0, metavar="NSTEPS",
                     help="run both forms NSTEPS steps and report the FP32 form's error")
     ap.add_argument("--solver", default=None, help="hlld or hll")
+    ap.add_argument("--monitor", type=int, default=0, metavar="NSTEPS",
+                    help="long precision-form run with both solvers, diagnostics every --monitor-every steps")
+    ap.add_argument("--monitor-every", type=int, default=100)
+    ap.add_argument("--monitor-forms", default="fp32", help="fp32, fp64 or fp32,fp64")
+    ap.add_argument("--monitor-solvers", default="hlld,hll")
     ap.add_argument("--batch-check", type=int, default=0, metavar="NSTEPS")
     args = ap.parse_args()
     if args.precision_report:
         return precision_report(args)
+    if args.monitor:
+        return monitor_run(args)
     if args.workload.startswith("batch"):
         return batch_bench(args)
     rank, world, local = rank_info()
