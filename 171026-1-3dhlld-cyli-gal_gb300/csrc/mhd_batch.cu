@@ -415,7 +415,7 @@ struct mhd_batch {
 #define BCK(call)                                                                          \
     do {                                                                                   \
         cudaError_t e_ = (call);                                                           \
-        if (e_ != cudaSuccess) return e_ == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; \
+        if (e_ != cudaSuccess) { cudaGetLastError(); return e_ == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; } \
     } while (0)
 
 static int ceil_div(int a, int b) { return (a + b - 1) / b; }

@@ -77,10 +77,13 @@ static cudaError_t prof_end(mhd_ctx *ctx)
         CK(prof_end(ctx));            \
     } while (0)
 
+/* a failed call's error is returned and the runtime's last-error latch is
+ * cleared, so the next launch check does not report it a second time */
 #define CK(call)                                   \
     do {                                           \
         cudaError_t e_ = (call);                   \
         if (e_ != cudaSuccess) {                   \
+            cudaGetLastError();                    \
             if (ctx) ctx->last_cuda = e_;          \
             return MHD_ERR_CUDA;                   \
         }                                          \
@@ -165,6 +168,11 @@ static void free_all(mhd_ctx *ctx)
                    ctx->rhofloor, ctx->F, ctx->Gf, ctx->H, ctx->Uraw, ctx->d_sc, ctx->d_trig, ctx->d_trigf,
                    ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run, ctx->d_snap};
     if (ctx->h_snap) cudaFreeHost(ctx->h_snap);
+    for (int q = 0; q < NSTAGE; q++) {
+        if (ctx->ev_cp[q]) cudaEventDestroy(ctx->ev_cp[q]);
+        if (ctx->ev_cvt[q]) cudaEventDestroy(ctx->ev_cvt[q]);
+        if (ctx->st_cp[q]) { cudaStreamSynchronize(ctx->st_cp[q]); cudaStreamDestroy(ctx->st_cp[q]); }
+    }
     if (ctx->ev_snap) cudaEventDestroy(ctx->ev_snap);
     if (ctx->ev_host) cudaEventDestroy(ctx->ev_host);
     if (ctx->st_io) cudaStreamDestroy(ctx->st_io);
@@ -297,6 +305,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     do {                                           \
         cudaError_t e_ = (call);                   \
         if (e_ != cudaSuccess) {                   \
+            cudaGetLastError();                    \
             free_all(ctx); delete ctx;             \
             return e_ == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; \
         }                                          \
@@ -364,7 +373,14 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     CKC(cudaMalloc((void **)&ctx->d_cnt, 3 * 3 * sizeof(int)));
     CKC(cudaMallocHost((void **)&ctx->h_cnt, 3 * 3 * sizeof(int)));
     ctx->stage_n = 1LL << 24;
-    if (ctx->fp32) CKC(cudaMalloc((void **)&ctx->d_stage, ctx->stage_n * sizeof(double)));
+    if (ctx->fp32) {
+        CKC(cudaMalloc((void **)&ctx->d_stage, NSTAGE * ctx->stage_n * sizeof(double)));
+        for (int q = 0; q < NSTAGE; q++) {
+            CKC(cudaStreamCreateWithFlags(&ctx->st_cp[q], cudaStreamNonBlocking));
+            CKC(cudaEventCreateWithFlags(&ctx->ev_cp[q], cudaEventDisableTiming));
+            CKC(cudaEventCreateWithFlags(&ctx->ev_cvt[q], cudaEventDisableTiming));
+        }
+    }
     CKC(cudaStreamSynchronize(ctx->st));
 #undef CKC
     *out = ctx;
@@ -391,10 +407,19 @@ static int put_state(mhd_ctx *ctx, void *dst, const double *src, long long n)
         CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
         return MHD_OK;
     }
-    for (long long off = 0; off < n; off += ctx->stage_n) {
+    /* NSTAGE staging buffers, each with its own copy stream, so several copy
+     * engines move chunks at once while the context stream converts the ones
+     * that have arrived; all ordering is by events */
+    int b = 0;
+    for (long long off = 0; off < n; off += ctx->stage_n, b = (b + 1) % NSTAGE) {
         long long m = n - off < ctx->stage_n ? n - off : ctx->stage_n;
-        CK(cudaMemcpyAsync(ctx->d_stage, src + off, m * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-        LAUNCH(PK_CVT, launch_cvt(ctx->d_stage, (float *)dst + off, m, ctx->st));
+        double *buf = ctx->d_stage + b * ctx->stage_n;
+        CK(cudaStreamWaitEvent(ctx->st_cp[b], ctx->ev_cvt[b], 0));   /* the buffer's last reader is done */
+        CK(cudaMemcpyAsync(buf, src + off, m * sizeof(double), cudaMemcpyHostToDevice, ctx->st_cp[b]));
+        CK(cudaEventRecord(ctx->ev_cp[b], ctx->st_cp[b]));
+        CK(cudaStreamWaitEvent(ctx->st, ctx->ev_cp[b], 0));
+        LAUNCH(PK_CVT, launch_cvt(buf, (float *)dst + off, m, ctx->st));
+        CK(cudaEventRecord(ctx->ev_cvt[b], ctx->st));
     }
     return MHD_OK;
 }
@@ -405,12 +430,20 @@ static int get_state(mhd_ctx *ctx, double *dst, const void *src, long long n)
         CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
         return MHD_OK;
     }
-    for (long long off = 0; off < n; off += ctx->stage_n) {
+    /* conversions on the context stream feed NSTAGE buffers whose copies out
+     * run on their own copy streams; the context stream then waits for all */
+    int b = 0;
+    for (long long off = 0; off < n; off += ctx->stage_n, b = (b + 1) % NSTAGE) {
         long long m = n - off < ctx->stage_n ? n - off : ctx->stage_n;
-        LAUNCH(PK_CVT, launch_cvt_back((const float *)src + off, ctx->d_stage, m, ctx->st));
-        CK(cudaMemcpyAsync(dst + off, ctx->d_stage, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-        CK(cudaStreamSynchronize(ctx->st));
+        double *buf = ctx->d_stage + b * ctx->stage_n;
+        CK(cudaStreamWaitEvent(ctx->st, ctx->ev_cp[b], 0));      /* the buffer's last copy is done */
+        LAUNCH(PK_CVT, launch_cvt_back((const float *)src + off, buf, m, ctx->st));
+        CK(cudaEventRecord(ctx->ev_cvt[b], ctx->st));
+        CK(cudaStreamWaitEvent(ctx->st_cp[b], ctx->ev_cvt[b], 0));
+        CK(cudaMemcpyAsync(dst + off, buf, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->st_cp[b]));
+        CK(cudaEventRecord(ctx->ev_cp[b], ctx->st_cp[b]));
     }
+    for (int q = 0; q < NSTAGE; q++) CK(cudaStreamWaitEvent(ctx->st, ctx->ev_cp[q], 0));
     return MHD_OK;
 }
 
@@ -445,6 +478,7 @@ extern "C" int mhd_upload_state(mhd_ctx *ctx, const double *U, const double *V)
     if ((rc = put_state(ctx, ctx->U, U, 9 * ctx->nc))) return rc;
     ctx->vcur = 0;
     if ((rc = put_state(ctx, ctx->Va, V, 9 * ctx->nc))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));   /* the caller's arrays are free again on return */
     return MHD_OK;
 }
 

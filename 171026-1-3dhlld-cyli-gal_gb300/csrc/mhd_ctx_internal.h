@@ -13,6 +13,8 @@
 
 #include "mhd_launch.h"
 
+#define NSTAGE 4   /* staging buffers (and copy streams) of the precision form's host transfers */
+
 struct mhd_ctx {
     int device;
     cudaStream_t st;
@@ -35,8 +37,10 @@ struct mhd_ctx {
     mhd::MaxLoc *d_part, *h_part;
     int npart;
     int *d_cnt, *h_cnt;
-    double *d_stage;
+    double *d_stage;             /* NSTAGE staging buffers of stage_n doubles (precision form) */
     long long stage_n;
+    cudaStream_t st_cp[NSTAGE];  /* one copy stream per staging buffer */
+    cudaEvent_t ev_cp[NSTAGE], ev_cvt[NSTAGE];
     std::vector<double> hx, hy, hz, hspL;
     double omdiff;
     int uploaded;
