@@ -29,7 +29,7 @@ using namespace mhd;
 
 
 enum { PK_FLUX_R = 0, PK_FLUX_PHI = 1, PK_FLUX_Z = 2, PK_UPDATE = 3, PK_GHOST = 4, PK_SETDT = 5, PK_TRIG = 6,
-       PK_CVT = 7, PK_STAGE = 8 };
+       PK_CVT = 7, PK_STAGE = 8, PK_ZUPDATE = 9 };
 static const int MAXSLOT = 256;
 
 /* fold the recorded event pairs into the per-kind totals */
@@ -595,8 +595,12 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     a.Vout = (T *)vnext_ptr(ctx); a.Uraw = (T *)ctx->Uraw;
     a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.trigf = ctx->d_trigf; a.kind = kind; a.last = last; a.counters = counters;
     a.Vinit = Vinit;
-    if (ctx->fused) {
+    if (ctx->fused == 1) {
         LAUNCH(PK_STAGE, launch_stage(ctx->G, a, ctx->stage_tj, ctx->stage_seg, ctx->st));
+    } else if (ctx->fused == 2) {
+        LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
+        LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
+        LAUNCH(PK_ZUPDATE, launch_zupdate(ctx->G, a, ctx->st));
     } else {
         LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
         LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
@@ -1045,7 +1049,7 @@ extern "C" int mhd_prof_enable(mhd_ctx *ctx, int on)
 
 extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
 {
-    if (!ctx || (fused != 0 && fused != 1) || tj != 7 || seg < 1) return MHD_ERR_ARG;
+    if (!ctx || fused < 0 || fused > 2 || tj != 7 || seg < 1) return MHD_ERR_ARG;
     ctx->fused = fused;
     ctx->stage_tj = tj;
     ctx->stage_seg = seg;

@@ -44,6 +44,7 @@ struct StageArgs {
     cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                         \
     cudaError_t launch_stage(const Geom &G, const StageArgs<T> &a, int tj, int seg, cudaStream_t st);        \
     cudaError_t prepare_stage(T *); /* shared-memory attribute of the fused kernels */                       \
+    cudaError_t launch_zupdate(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                      \
     cudaError_t launch_setdt(const Geom &G, const T *V, MaxLoc *part, int nblk, cudaStream_t st);            \
     cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
                               const float *trigf, double *S, cudaStream_t st);                               \

@@ -454,7 +454,8 @@ class Disc:
     def download_into(self, U, V):
         check(lib().mhd_download(self.h, _ptr(U), _ptr(V)), "mhd_download")
 
-    PROF_KINDS = ["flux_r", "flux_phi", "flux_z", "update", "ghost", "setdt", "trig", "convert", "stage"]
+    PROF_KINDS = ["flux_r", "flux_phi", "flux_z", "update", "ghost", "setdt", "trig", "convert", "stage",
+                  "zupdate"]
 
     def prof(self, on=True):
         check(lib().mhd_prof_enable(self.h, 1 if on else 0), "mhd_prof_enable")
@@ -473,9 +474,10 @@ class Disc:
         check(lib().mhd_checkpoint_wait(self.h), "mhd_checkpoint_wait")
 
     def set_stage_shape(self, fused=True, tj=7, seg=32):
-        """fused: one kernel per stage for fluxes + update; tj (7) j-cells
-        per tile, seg r-cells per run (mhd_set_stage_shape)."""
-        check(lib().mhd_set_stage_shape(self.h, 1 if fused else 0, int(tj), int(seg)), "mhd_set_stage_shape")
+        """fused: 0/False split kernels, 1/True one fused stage kernel (tj = 7
+        j-cells per tile, seg r-cells per run), 2 z fluxes fused into the
+        update (mhd_set_stage_shape)."""
+        check(lib().mhd_set_stage_shape(self.h, int(fused), int(tj), int(seg)), "mhd_set_stage_shape")
 
     def launches(self):
         return int(lib().mhd_launch_count(self.h))

@@ -235,15 +235,17 @@ int mhd_checkpoint_wait(mhd_ctx *ctx);
 /* Per-kernel timing with CUDA events recorded around every launch on the
  * context's stream (off by default; enabling resets the totals).  Kinds:
  * 0 flux r, 1 flux phi, 2 flux z, 3 update, 4 ghost fill, 5 CFL reduction,
- * 6 arm-phase table, 7 state conversion, 8 fused stage (fluxes + update). */
-#define MHD_PROF_NKIND 9
+ * 6 arm-phase table, 7 state conversion, 8 fused stage (fluxes + update),
+ * 9 z fluxes + update. */
+#define MHD_PROF_NKIND 10
 int mhd_prof_enable(mhd_ctx *ctx, int on);
 int mhd_prof_read(mhd_ctx *ctx, double ms[MHD_PROF_NKIND], long long launches[MHD_PROF_NKIND]);
-/* How a stage runs.  fused = 0 (default): three flux kernels write F, G, H to
- * device memory and an update kernel reads them; fused = 1: one kernel forms
- * the r, phi and z face fluxes on chip and updates the cells (tile 32 k-cells
- * x tj j-cells, tj = 7, marching over runs of seg cells in r).  Both give the
- * same bits in the plain form; on GB300 the split form is the faster one. */
+/* How a stage runs.  fused = 0: three flux kernels write F, G, H to device
+ * memory and an update kernel reads them; fused = 2: the r and phi flux
+ * kernels, then one kernel forms the z fluxes in registers and updates the
+ * cells; fused = 1: one kernel forms all fluxes on chip and updates the cells
+ * (tile 32 k-cells x tj j-cells, tj = 7, marching over runs of seg cells in
+ * r).  All give the same bits in the plain form. */
 int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg);
 /* Kernels this context has launched since creation. */
 long long mhd_launch_count(const mhd_ctx *ctx);

@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 
 # (nr, nphi, nz): one tile; ragged tiles in k (70 = 2x32 + 6) and j; runs in r
 SHAPES = [(20, 12, 14), (40, 24, 70)]
-STAGE = [(True, 7, 32), (True, 7, 5), (True, 7, 1), (False, 7, 32)]
+# (fused, tj, seg): 1 = one fused stage kernel, 2 = z fluxes fused into the update, 0 = split
+STAGE = [(1, 7, 32), (1, 7, 5), (1, 7, 1), (2, 7, 32), (0, 7, 32)]
 
 
 def same(a, b):
@@ -58,8 +59,8 @@ def test_fp64_stage_shapes_bitwise(M, P, variant, dims):
 def test_fp32_fused_matches_split(M, variant):
     grid, params, U, V = make_case(M, variant, (40, 24, 70))
     p32 = M.default_params(**{k: v for k, v in params.as_dict().items() if k != "precision"}, precision="fp32")
-    Us, Vs, _ = run_disc(M, grid, p32, U, V, 5, (False, 7, 32))
-    for shape in STAGE[:3]:
+    Us, Vs, _ = run_disc(M, grid, p32, U, V, 5, (0, 7, 32))
+    for shape in [sh for sh in STAGE if sh[0] != 0]:
         Uf, Vf, _ = run_disc(M, grid, p32, U, V, 5, shape)
         err = rel_l1(Uf, Us)
         # m_z, B_r, B_z, psi start at (or near) zero: judged against the
@@ -79,16 +80,16 @@ def test_fp32_run_graph_follows_shape(M):
     grid, params, U, V = make_case(M, "rk3_minmod_hlld", (40, 24, 70))
     p32 = M.default_params(**{k: v for k, v in params.as_dict().items() if k != "precision"}, precision="fp32")
     ref = M.Disc(grid, p32)
-    ref.set_stage_shape(False, 7, 32)
+    ref.set_stage_shape(0, 7, 32)
     ref.upload(U, V)
     ref.run(2, 0.0)
     Ur, _ = ref.download()
     ref.close()
     d = M.Disc(grid, p32)
-    d.set_stage_shape(True, 7, 32)
+    d.set_stage_shape(1, 7, 32)
     d.upload(U, V)
     d.run(1, 0.0)                      # graph built with the fused shape
-    d.set_stage_shape(False, 7, 32)
+    d.set_stage_shape(0, 7, 32)
     d.upload(U, V)
     d.run(2, 0.0)                      # must run the split kernels now
     Ud, _ = d.download()
@@ -99,6 +100,6 @@ def test_fp32_run_graph_follows_shape(M):
 def test_stage_shape_rejects_bad_arguments(M):
     grid, params, U, V = make_case(M, "rk3_minmod_hlld", (20, 12, 14))
     d = M.Disc(grid, params)
-    for bad in [(2, 7, 32), (1, 3, 32), (1, 7, 0)]:
+    for bad in [(3, 7, 32), (1, 3, 32), (1, 7, 0)]:
         assert M.lib().mhd_set_stage_shape(d.h, *bad) == M.MHD_ERR_ARG
     d.close()
