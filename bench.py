@@ -518,17 +518,19 @@ def main():
         # fused stage: V, U^n, rhofloor, U and V out every stage, U^(k) in two of
         # the three RK3 stages (fluxes stay on chip)
         "stage": zones * (9 + 9 + 1 + 9 + 9 + 6) * s,
+        # z fluxes + update: the update's bytes less the H round trip
+        "zupdate": zones * (64 - 9) * s,
     }
-    achieved = per_launch[dom] / (dms / dn / 1e3) / 1e9 if dn else None
+    achieved = per_launch.get(dom, 0) / (dms / dn / 1e3) / 1e9 if dn else None
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-            "algorithmic_bytes_per_launch": per_launch[dom], "avg_launch_ms": dms / dn if dn else None,
+            "algorithmic_bytes_per_launch": per_launch.get(dom, 0), "avg_launch_ms": dms / dn if dn else None,
             "note": "stencil with no contraction: the FP32/FP64 pipes, not HBM, bound these kernels; "
                     "see profiles/ for pipe utilisation"}
     shares = {k: round(v[0] / tot, 4) for k, v in kern.items() if v[1]}
     nprof = max(3, min(args.steps, 5))
-    alg_step = sum(per_launch[k] * kern[k][1] for k in kern) / nprof   # algorithmic bytes per step
+    alg_step = sum(per_launch.get(k, 0) * kern[k][1] for k in kern) / nprof   # algorithmic bytes per step
 
     # ---- e2e through the C-ABI with host FP64 buffers ----
     e2e = None
