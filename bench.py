@@ -456,10 +456,10 @@ def main():
     cfg = {"workload": "%s: single disc %dx%dx%d (r in [0.1,1.5], phi in [0,2pi), z in [-0.5,0.5]), "
                        "beta=1, cooling on, HLLD, minmod, TVD-RK3, CFL 0.4, seeded 1%% perturbation"
                        % (args.workload, dims[0], dims[1], dims[2]),
-           "zones": zones, "l2": "state (>=2.5 GB) larger than L2; no flush needed",
-           "timed_path": "value: mhd_run, one CUDA graph per RK3 step (CFL reduction and dt on the device); "
-                         "kernel shares/roofline: a separate mhd_step pass with events around each launch; "
-                         "e2e: mhd_upload_state + mhd_step + mhd_download per step"}
+           "zones": zones, "l2": "state (>=2.5 GB) larger than L2; no flush needed"}
+    timed_path = ("value: mhd_run, one CUDA graph per RK3 step (CFL reduction and dt on the device); "
+                  "kernel shares/roofline: a separate mhd_step pass with events around each launch; "
+                  "e2e: mhd_upload_state + mhd_step + mhd_download per step")
 
     if args.impl == "reference":
         if rank != 0:
@@ -574,7 +574,8 @@ def main():
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic (seeded disc initial state; no public dataset exists)",
-               "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
+               "config": cfg, "timed_path": timed_path, "e2e": e2e, "roofline": roof, "cpu_baseline": cb,
+               "clocks": clocks,
                "gpu_launches": launches,
                "kernel_share": shares,
                "fp64": {"value": v64, "unit": "zone-updates/s", "steps": f64_steps,
