@@ -100,9 +100,9 @@ __device__ __forceinline__ void add_counts(int a, int b, int c, int *counters)
 
 /* bounded wait until *flag >= target; false (and the error flag set) if the
  * limit runs out */
-__device__ __forceinline__ bool wait_at_least(int *flag, int target, int *err)
+__device__ __forceinline__ bool wait_at_least(int *flag, int target, int *err, int limit)
 {
-    for (int it = 0; it < MHD_SPIN_LIMIT; it++) {
+    for (int it = 0; it < limit; it++) {
         if (atomicAdd(flag, 0) >= target) {
             __threadfence();
             return true;
@@ -128,7 +128,7 @@ __device__ __forceinline__ void load_geom(Geom &sG, const Geom &G)
 template <int BT, int MINB, int TI, int TJ, int TK>
 __global__ void __launch_bounds__(BT, MINB)
 batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ tiles, int ntiles, int *head,
-                   int *done, int ndisc, int *err, int kind, int last, int parity, int stage)
+                   int *done, int ndisc, int *err, int spin, int kind, int last, int parity, int stage)
 {
     __shared__ int s_t, s_ok;
     __shared__ Geom sG;
@@ -143,8 +143,8 @@ batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ 
         load_geom(sG, D.G);
         if (threadIdx.x == 0) {
             int ok = 1;
-            if (code == 3) ok = wait_at_least(&done[d], D.nflux, err);
-            else if (code == 4) ok = wait_at_least(&done[ndisc + d], D.nupd, err);
+            if (code == 3) ok = wait_at_least(&done[d], D.nflux, err, spin);
+            else if (code == 4) ok = wait_at_least(&done[ndisc + d], D.nupd, err, spin);
             s_ok = ok;
         }
         __syncthreads();
@@ -410,6 +410,8 @@ struct mhd_batch {
     cudaGraphExec_t gx[2];
     int graph_ready, parity;
     long long launches;
+    int spin_limit;             /* iterations of a bounded device-side wait */
+    int stall_disc;             /* test hook: this disc's flux count is never reached (-1: none) */
 };
 
 #define BCK(call)                                                                          \
@@ -437,6 +439,7 @@ static int build_tiles(mhd_batch *b, TileCfg c)
             for (int l = 0; l < nt; l++) tl.push_back(make_uint2(d, ((unsigned)dir << 28) | (unsigned)l));
             D.nflux += nt;
         }
+        if (d == b->stall_disc) D.nflux += 1;   /* the update tiles' wait can then only time out */
     }
     for (int d = 0; d < n; d++) {
         DiscDev &D = b->hd[d];
@@ -487,7 +490,8 @@ static cudaError_t launch_stage(mhd_batch *b, int *head, int *done, int kind, in
 #define MHD_LAUNCH(V, BT, MB, TI, TJ, TK)                                                                  \
     case V:                                                                                                \
         batch_stage_kernel<BT, MB, TI, TJ, TK><<<nb, BT, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, done, \
-                                                                     b->n, b->derr, kind, last, parity, stage); \
+                                                                     b->n, b->derr, b->spin_limit, kind, last,    \
+                                                                     parity, stage);                              \
         break;
         MHD_BATCH_VARIANTS(MHD_LAUNCH)
 #undef MHD_LAUNCH
@@ -696,6 +700,8 @@ extern "C" int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *
     mhd_batch *b = new (std::nothrow) mhd_batch();
     if (!b) return MHD_ERR_NOMEM;
     b->n = n;
+    b->spin_limit = MHD_SPIN_LIMIT;
+    b->stall_disc = -1;
     b->ctx.assign(n, NULL);
     b->stopped.assign(n, 0);
     int fp32 = params[0].precision == MHD_PREC_FP32;
@@ -843,6 +849,21 @@ extern "C" int mhd_batch_set_mode(mhd_batch *b, int mode, int arg)
     if (b->st) BCK(cudaStreamSynchronize(b->st));
     b->phased = mode == 1;
     b->discgraph = mode == 2;
+    b->graph_ready = 0;
+    return MHD_OK;
+}
+
+extern "C" int mhd_batch_debug_stall(mhd_batch *b, int disc, int spin_limit)
+{
+    if (!b || !b->persistent || disc < -1 || disc >= b->n || (disc >= 0 && spin_limit < 1)) return MHD_ERR_ARG;
+    if (b->st) BCK(cudaStreamSynchronize(b->st));
+    b->stall_disc = disc;
+    b->spin_limit = disc >= 0 ? spin_limit : MHD_SPIN_LIMIT;
+    b->phased = 0;
+    b->discgraph = 0;
+    int rc = build_tiles(b, b->cfg);
+    if (rc) return rc;
+    b->nblk_stage = stage_blocks(b->cfg);
     b->graph_ready = 0;
     return MHD_OK;
 }

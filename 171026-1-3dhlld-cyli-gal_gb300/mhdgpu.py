@@ -17,6 +17,7 @@ LIBPATH = os.path.join(PKG, "lib", "libmhdgpu.so")
 MHD_OK = 0
 MHD_ERR_ARG = -1
 MHD_ERR_DT = -3
+MHD_ERR_TIMEOUT = -6
 MHD_ERR_IO = -8
 LIMITER = {"minmod": 0, "mc": 1, "vanleer": 2, "superbee": 3}
 SOURCE = {"spiral": 0, "axi": 1, "uniformgz": 2, "none": 3}
@@ -128,6 +129,7 @@ def lib():
         "mhd_batch_step": (C.c_int, [vp, C.c_int, DP, IP]),
         "mhd_batch_tune": (C.c_int, [vp, IP]),
         "mhd_batch_set_mode": (C.c_int, [vp, C.c_int, C.c_int]),
+        "mhd_batch_debug_stall": (C.c_int, [vp, C.c_int, C.c_int]),
         "mhd_upload_state": (C.c_int, [vp, vp, vp]),
         "mhd_prof_enable": (C.c_int, [vp, C.c_int]),
         "mhd_set_stage_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
@@ -542,6 +544,9 @@ class Batch:
         best = np.zeros(5, dtype=np.int32)
         check(lib().mhd_batch_tune(self.h, best), "mhd_batch_tune")
         return tuple(int(v) for v in best)
+
+    def debug_stall(self, disc, spin_limit=4096):
+        check(lib().mhd_batch_debug_stall(self.h, int(disc), int(spin_limit)), "mhd_batch_debug_stall")
 
     def set_mode(self, mode, arg=0):
         """0 persistent (tile candidate arg), 1 phased, 2 disc graph on arg branches."""

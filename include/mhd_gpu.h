@@ -294,6 +294,14 @@ int mhd_batch_tune(mhd_batch *b, int *best);
 /* Pick the precision form's batch mode directly: 0 persistent with compiled
  * tile candidate arg, 1 phased, 2 disc graph on arg branches (1..64). */
 int mhd_batch_set_mode(mhd_batch *b, int mode, int arg);
+/* Test hook for the persistent mode's bounded waits (an update tile waits,
+ * with an iteration limit, for its disc's flux tiles): with disc >= 0 that
+ * disc's flux count is set one above what the stage produces and the limit
+ * to spin_limit, so the next step's wait runs out -- no fault, no hang -- and
+ * mhd_batch_step returns MHD_ERR_TIMEOUT (the state of that step is then
+ * undefined: upload again).  disc = -1 restores normal operation.  Selects
+ * the persistent mode. */
+int mhd_batch_debug_stall(mhd_batch *b, int disc, int spin_limit);
 
 /* ---- allocation-free CFL reduction -------------------------------------- */
 /* No counterpart in the reference.  For callers that may not call cudaMalloc

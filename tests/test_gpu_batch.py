@@ -162,3 +162,38 @@ def test_batch_modes_match_single_disc_runs(M, mode, arg):
     with pytest.raises(M.MhdError):
         b.set_mode(2, 0)
     b.close()
+
+
+def test_batch_bounded_wait_times_out_and_recovers(M):
+    """The persistent kernel's waits are bounded: a flux count that is never
+    reached (test hook) ends the step with MHD_ERR_TIMEOUT after the short
+    limit, with no fault; with the hook cleared and the state uploaded again
+    the batch steps normally."""
+    cases = make_discs(M)
+    b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
+    b.set_mode(0, 0)
+    for d, (g, p, U, V) in enumerate(cases):
+        b.upload(d, U, V)
+    b.debug_stall(1, 4096)
+    with pytest.raises(M.MhdError) as e:
+        b.step(1, np.zeros(len(cases)))
+    assert e.value.code == M.MHD_ERR_TIMEOUT
+    b.debug_stall(-1)
+    for d, (g, p, U, V) in enumerate(cases):
+        b.upload(d, U, V)
+    t, st = b.step(2, np.zeros(len(cases)))
+    assert np.all(st == 0)
+    for d, (g, p, U, V) in enumerate(cases):
+        s = M.Disc(g, p)
+        s.upload(U, V)
+        ts = s.run(2, 0.0)
+        Us, _ = s.download()
+        Ub, _ = b.download(d)
+        assert abs(ts - t[d]) <= 1e-12 * ts
+        err = rel_l1(Ub[:8], Us[:8])
+        bscale = np.abs(Us[4:7]).sum()
+        for m in (4, 6):
+            err[m] = np.abs(Ub[m] - Us[m]).sum() / bscale
+        assert np.all(err <= 1e-6), (d, err)
+        s.close()
+    b.close()
