@@ -24,6 +24,11 @@
  * state and restores it.  The halo is read through L1 from global memory, so
  * its depth is the stencil's (2 cells) for every tile shape.
  *
+ * Two other modes are tuner candidates: phased (one launch per stage phase
+ * over all discs) and the disc graph (each disc's own single-disc step, the
+ * discs dealt to parallel stream branches of one graph), which is the fastest
+ * on the 64-disc workload.
+ *
  * Precision form only (FP32 + FP64 repair, the per-cell code of the
  * single-disc kernels); a batch of plain FP64 discs is stepped disc by disc
  * through mhd_step, each bit-identical to the reference.

@@ -3,8 +3,9 @@
  * instantiated once per precision form by mhd_fp64.cu / mhd_fp32.cu (which
  * differ only in compile flags).
  *
- * One RK stage = flux(r) + flux(phi) + flux(z) + update + ghost, or the fused
- * stage kernel (all four in one launch) + ghost:
+ * One RK stage = flux(r) + flux(phi) + flux(z: boundary faces, interior
+ * faces) + update + ghost (the default), or flux(r) + flux(phi) + z fluxes
+ * fused into the update + ghost, or the fused stage kernel + ghost:
  *   flux    one thread per face the update reads; reconstruction of the two
  *           adjacent cells, Riemann solver, GLM flux -> F/G/H[9][cells]
  *   update  one thread per interior cell: sources, the stage's conservative

@@ -137,7 +137,7 @@ def test_precision_form_against_fp64(M, P):
         assert rc == 0
     Ug, Vg = d.download()
     err = rel_l1(Ug, Uo)
-    # psi starts at 0 and stays tiny: judge it against the field scale instead
+    # psi starts at 0 and stays tiny: measure it against the field scale instead
     err[8] = np.abs(Ug[8] - Uo[8]).sum() / max(np.abs(Uo[4:7]).sum(), 1e-300)
     assert np.all(err[:8] < 1e-4), err
     d.close()

@@ -61,7 +61,7 @@ def test_shipped_precision_form(M, shipped):
     err = rel_l1(Ug, Uo)
     # GalacticDisc3 is an equilibrium with v_r = v_z = 0 and only B_phi: after
     # a few steps m_r, m_z, B_r, B_z, psi are the small residue of cancelling
-    # forces, so they are judged against the momentum and field scales
+    # forces, so they are measured against the momentum and field scales
     x = grid.arr("x", grid.ixmax)[:, None, None]
     mscale = np.abs(Uo[2] / x).sum()
     bscale = max(np.abs(Uo[4:7]).sum(), 1e-300)

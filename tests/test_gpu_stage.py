@@ -63,7 +63,7 @@ def test_fp32_fused_matches_split(M, variant):
     for shape in [sh for sh in STAGE if sh[0] != 0]:
         Uf, Vf, _ = run_disc(M, grid, p32, U, V, 5, shape)
         err = rel_l1(Uf, Us)
-        # m_z, B_r, B_z, psi start at (or near) zero: judged against the
+        # m_z, B_r, B_z, psi start at (or near) zero: measured against the
         # momentum and field scales
         x = grid.arr("x", grid.ixmax)[:, None, None]
         mscale = np.abs(Us[2] / x).sum()
