@@ -189,6 +189,9 @@ static void free_all(mhd_ctx *ctx)
         if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
     for (int q = 0; q < 2; q++)
         if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->st_aux) { cudaStreamSynchronize(ctx->st_aux); cudaStreamDestroy(ctx->st_aux); }
     if (ctx->st) cudaStreamDestroy(ctx->st);
 }
 
@@ -312,6 +315,9 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     } while (0)
 
     CKC(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+    CKC(cudaStreamCreateWithFlags(&ctx->st_aux, cudaStreamNonBlocking));
+    CKC(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    CKC(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     CKC(ctx->fp32 ? prepare_stage((float *)0) : prepare_stage((double *)0));
     CKC(cudaMalloc((void **)&ctx->dtab, T.size() * sizeof(double)));
     CKC(cudaMalloc((void **)&ctx->ftab, TF.size() * sizeof(float)));
@@ -604,7 +610,15 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     } else {
         LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
         LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
-        LAUNCH(PK_FLUX_Z, launch_flux(2, ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), false, ctx->st));
+        /* the z boundary faces (latency-bound) on the side stream, beside the
+         * interior z faces (issue-bound); the update waits for both */
+        CK(cudaEventRecord(ctx->ev_fork, ctx->st));
+        CK(cudaStreamWaitEvent(ctx->st_aux, ctx->ev_fork, 0));
+        CK(launch_zedge(ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), ctx->st_aux));
+        ctx->launches++;
+        CK(cudaEventRecord(ctx->ev_join, ctx->st_aux));
+        LAUNCH(PK_FLUX_Z, launch_flux_zinterior(ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), ctx->st));
+        CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
         LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
     }
     LAUNCH(PK_GHOST, launch_ghost(ctx->G, a, ctx->st));

@@ -18,6 +18,8 @@
 struct mhd_ctx {
     int device;
     cudaStream_t st;
+    cudaStream_t st_aux;         /* the z boundary faces beside the interior z faces */
+    cudaEvent_t ev_fork, ev_join;
     mhd_params p;
     int ix, jy, kz, ixmax, jymax, kzmax, irin;
     long long nc;

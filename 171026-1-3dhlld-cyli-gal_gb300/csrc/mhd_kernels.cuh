@@ -681,21 +681,39 @@ static inline void grid3(int nk, int nj, int ni, dim3 &grid, dim3 &block)
     grid = dim3((nk + bx - 1) / bx, (nj + by - 1) / by, ni);
 }
 
+/* the z boundary faces (face 0 and kzmax-2) of a face box, if it has them */
+static inline void zedge_sides(const Geom &G, const Box &b, int &lo, int &hi)
+{
+    lo = b.k0 == 0;
+    hi = b.k1 > G.kzmax - 2 && b.k0 <= G.kzmax - 2 && G.kzmax - 2 > 0;
+}
+
+template <typename T>
+cudaError_t launch_zedge_t(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, Box b,
+                           bool reflayout, cudaStream_t st)
+{
+    if (b.i1 <= b.i0 || b.j1 <= b.j0 || b.k1 <= b.k0) return cudaSuccess;
+    int lo, hi;
+    zedge_sides(G, b, lo, hi);
+    if (!lo && !hi) return cudaSuccess;
+    long long n = (long long)(b.i1 - b.i0) * (b.j1 - b.j0) * (lo + hi);
+    if (reflayout) flux_zedge_kernel<T, true><<<nblocks(n, 128), 128, 0, st>>>(G, V, Vinit, sc, F, b, lo, hi);
+    else flux_zedge_kernel<T, false><<<nblocks(n, 128), 128, 0, st>>>(G, V, Vinit, sc, F, b, lo, hi);
+    return cudaGetLastError();
+}
+
+/* dir 2 with edges = false leaves the boundary z faces to launch_zedge_t */
 template <typename T>
 cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,
-                          Box b, bool reflayout, cudaStream_t st)
+                          Box b, bool reflayout, cudaStream_t st, bool edges = true)
 {
     if (b.i1 <= b.i0 || b.j1 <= b.j0 || b.k1 <= b.k0) return cudaSuccess;
     if (dir == 2) {
         /* boundary z faces in their own launch, the rest below */
-        const int lo = b.k0 == 0, hi = b.k1 > G.kzmax - 2 && b.k0 <= G.kzmax - 2 && G.kzmax - 2 > 0;
-        if (lo || hi) {
-            long long n = (long long)(b.i1 - b.i0) * (b.j1 - b.j0) * (lo + hi);
-            if (reflayout)
-                flux_zedge_kernel<T, true><<<nblocks(n, 128), 128, 0, st>>>(G, V, Vinit, sc, F, b, lo, hi);
-            else
-                flux_zedge_kernel<T, false><<<nblocks(n, 128), 128, 0, st>>>(G, V, Vinit, sc, F, b, lo, hi);
-            cudaError_t e = cudaGetLastError();
+        int lo, hi;
+        zedge_sides(G, b, lo, hi);
+        if (edges && (lo || hi)) {
+            cudaError_t e = launch_zedge_t<T>(G, V, Vinit, sc, F, b, reflayout, st);
             if (e != cudaSuccess) return e;
         }
         if (lo) b.k0 = 1;
@@ -824,6 +842,16 @@ cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream
                             Box b, bool reflayout, cudaStream_t st)                                          \
     {                                                                                                        \
         return launch_flux_t<T>(dir, G, V, Vinit, sc, F, b, reflayout, st);                                  \
+    }                                                                                                        \
+    cudaError_t launch_flux_zinterior(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,      \
+                                      T *F, Box b, cudaStream_t st)                                          \
+    {                                                                                                        \
+        return launch_flux_t<T>(2, G, V, Vinit, sc, F, b, false, st, false);                                 \
+    }                                                                                                        \
+    cudaError_t launch_zedge(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, Box b,  \
+                             cudaStream_t st)                                                                \
+    {                                                                                                        \
+        return launch_zedge_t<T>(G, V, Vinit, sc, F, b, false, st);                                          \
     }                                                                                                        \
     cudaError_t launch_states(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,     \
                               T *Vl, T *Vr, Box b, cudaStream_t st)                                          \

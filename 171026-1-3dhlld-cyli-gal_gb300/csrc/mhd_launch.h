@@ -40,6 +40,10 @@ struct StageArgs {
                             Box b, bool reflayout, cudaStream_t st);                                         \
     cudaError_t launch_states(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,     \
                               T *Vl, T *Vr, Box b, cudaStream_t st);                                         \
+    cudaError_t launch_flux_zinterior(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,      \
+                                      T *F, Box b, cudaStream_t st);                                         \
+    cudaError_t launch_zedge(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, Box b,  \
+                             cudaStream_t st);                                                               \
     cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                        \
     cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                         \
     cudaError_t launch_stage(const Geom &G, const StageArgs<T> &a, int tj, int seg, cudaStream_t st);        \
