@@ -232,7 +232,7 @@ batch_setdt_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ 
             float t1 = sqrtf(v2 + ((float)MHD_GM * v7 + b2) / v0) / G.f.minlength[(long long)i * G.kzmax + k];
             int cl = G.cooling ? cooling_rate_f(v0, v7) : 0;
             float tc = (2.0f * ((v0 * v0 * (float)cl) / (1.5f * v7)));
-            double tmp = (double)rmax<float>(t1, tc);
+            double tmp = (t1 != t1 || tc != tc) ? (double)INFINITY : (double)rmax<float>(t1, tc);
             if (tmp > best.v && tmp > 0.0) { best.v = tmp; best.q = q; }
         }
     }
@@ -249,7 +249,7 @@ batch_setdt_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ 
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = better(b, sm[w]);
         if (b.q >= 0) {
             const int k = (int)(b.q % G.kzmax), i = (int)(b.q / ((long long)G.kzmax * G.jymax));
-            b.v = cfl_rate64<float>(G, V, i, b.q, k);
+            b.v = cfl_rate64_strict<float>(G, V, i, b.q, k);
         }
         D.part[local] = b;
     }

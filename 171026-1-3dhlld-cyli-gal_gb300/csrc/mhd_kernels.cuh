@@ -576,9 +576,31 @@ __device__ __forceinline__ double cfl_rate64(const Geom &G, const T *__restrict_
     return rmax<double>(t1, tc);
 }
 
+/* The precision form's CFL rate of one cell in FP64: cfl_rate64 except that
+ * a NaN rate (an invalid state) counts as infinite, so dt becomes 0 and the
+ * dt guard stops the run at once.  The plain form keeps the reference's
+ * semantics, where a NaN rate never wins (max() and the comparison of
+ * setdt.h:57,60 are false for NaN). */
+template <typename T>
+__device__ __forceinline__ double cfl_rate64_strict(const Geom &G, const T *__restrict__ V, int i, long long q,
+                                                    int k)
+{
+    const long long nc = G.nc;
+    double v0 = V[q], v1 = V[nc + q], v2v = V[2 * nc + q], v3 = V[3 * nc + q];
+    double v4 = V[4 * nc + q], v5 = V[5 * nc + q], v6 = V[6 * nc + q], v7 = V[7 * nc + q];
+    double v2 = v1 * v1 + v2v * v2v + v3 * v3;
+    double b2 = v4 * v4 + v5 * v5 + v6 * v6;
+    double t1 = sqrt(v2 + (MHD_GM * v7 + b2) / v0) / G.minlength[(long long)i * G.kzmax + k];
+    int cl = G.cooling ? cooling_rate(v0, v7) : 0;
+    double tc = (2.0 * ((v0 * v0 * cl) / (1.5 * v7)));
+    if (t1 != t1 || tc != tc) return INFINITY;
+    return rmax<double>(t1, tc);
+}
+
 /* Plain form: every cell in FP64, bit-identical to setdt.h.  Precision form:
  * cells are screened in FP32 and each block's winner is re-evaluated in FP64,
- * so the maximum (and dt) carries FP64 rounding of an FP32-selected cell. */
+ * so the maximum (and dt) carries FP64 rounding of an FP32-selected cell; a
+ * cell whose rate is NaN wins with an infinite rate (dt = 0: the guard). */
 template <typename T>
 __global__ void __launch_bounds__(256)
 setdt_kernel(Geom G, const T *__restrict__ V, MaxLoc *part)
@@ -603,7 +625,7 @@ setdt_kernel(Geom G, const T *__restrict__ V, MaxLoc *part)
                 float t1 = sqrtf(v2 + ((float)MHD_GM * v7 + b2) / v0) / (float)G.f.minlength[(long long)i * G.kzmax + k];
                 int cl = G.cooling ? cooling_rate_f(v0, v7) : 0;
                 float tc = (2.0f * ((v0 * v0 * (float)cl) / (1.5f * v7)));
-                tmp = (double)rmax<float>(t1, tc);
+                tmp = (t1 != t1 || tc != tc) ? (double)INFINITY : (double)rmax<float>(t1, tc);
             }
             /* the reference only takes a cell when its rate exceeds the running max (from 0) */
             if (tmp > best.v && tmp > 0.0) { best.v = tmp; best.q = q; }
@@ -622,7 +644,7 @@ setdt_kernel(Geom G, const T *__restrict__ V, MaxLoc *part)
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = better(b, sm[w]);
         if (sizeof(T) == 4 && b.q >= 0) {
             const int k = (int)(b.q % G.kzmax), i = (int)(b.q / ((long long)G.kzmax * G.jymax));
-            b.v = cfl_rate64<T>(G, V, i, b.q, k);
+            b.v = cfl_rate64_strict<T>(G, V, i, b.q, k);
         }
         part[blockIdx.x] = b;
     }

@@ -71,3 +71,27 @@ def test_diagnostics(M, prec):
     for k in want:
         assert abs(got[k] - want[k]) <= 1e-12 * max(abs(want[k]), 1e-300), (k, got[k], want[k])
     d.close()
+
+
+def test_invalid_cell_stops_the_precision_form(M):
+    """A NaN in the state: the precision form's CFL reduction counts its rate as
+    infinite, so the dt guard fires before any step is taken (mhd_step and
+    mhd_run); the plain form keeps the reference's Setdt, where a NaN rate never
+    wins the comparison (setdt.h:57,60), and steps on."""
+    grid, params, U, V = make_case(M, "rk3_minmod_hlld", (24, 16, 20))
+    Vb = V.copy()
+    Vb[7, 5, 7, 9] = np.nan          # a pressure inside the CFL range (i < ixmax - 11)
+    d = M.Disc(grid, fp32(M, params))
+    d.upload(U, Vb)
+    rc, t, dt, ch, cnt = d.step(0.0)
+    assert rc == M.MHD_ERR_DT and t == 0.0
+    d.upload(U, Vb)
+    with pytest.raises(M.MhdError) as e:
+        d.run(1, 0.0)
+    assert e.value.code == M.MHD_ERR_DT
+    d.close()
+    d64 = M.Disc(grid, params)
+    d64.upload(U, Vb)
+    rc, t, dt, ch, cnt = d64.step(0.0)
+    assert rc == 0 and np.isfinite(dt) and dt > 0
+    d64.close()
