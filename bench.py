@@ -543,8 +543,18 @@ def main():
         "zupdate": zones * (64 - 9) * s,
     }
     achieved = per_launch.get(dom, 0) / (dms / dn / 1e3) / 1e9 if dn else None
+    # DRAM bytes (read + write) per zone per launch from ncu captures at
+    # 256x256x128 (profiles/split_stage_fp32_256x256x128.md), scaled here by the
+    # zones of this workload; the update figure is a first-stage launch (the
+    # other two stages also read U^(k))
+    measured_traffic = {"update": (1.613456e9 + 0.626855e9) / 8388608,
+                        "flux_r": (0.338613e9 + 0.269102e9) / 8388608,
+                        "flux_phi": (0.331223e9 + 0.268120e9) / 8388608}
+    traffic = measured_traffic[dom] * zones if dom in measured_traffic else None
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+            "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 256x256x128, "
+                              "scaled by zones" if traffic else None,
             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
             "algorithmic_bytes_per_launch": per_launch.get(dom, 0), "avg_launch_ms": dms / dn if dn else None,
             "note": "stencil with no contraction: the FP32/FP64 pipes, not HBM, bound these kernels; "
