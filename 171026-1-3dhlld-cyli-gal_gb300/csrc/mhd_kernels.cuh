@@ -23,6 +23,11 @@
 #include "mhd_dev.cuh"
 #include "mhd_launch.h"
 
+/* faces per thread of the marched r and phi flux kernels */
+#ifndef MHD_MARCH_RUN
+#define MHD_MARCH_RUN 8
+#endif
+
 namespace mhd {
 
 /* ------------------------------------------------------------------------ */
@@ -60,6 +65,67 @@ flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const 
     const int i = b.i0 + blockIdx.z;
     if (k >= b.k1 || j >= b.j1) return;
     flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, i, j, k);
+}
+
+/* one face's flux into F (cell layout) or the reference's face layout */
+template <typename T, bool REFLAYOUT>
+__device__ __forceinline__ void store_face(const Geom &G, T *__restrict__ F, int i, int j, int k, const T Fo[9])
+{
+    if (REFLAYOUT) {
+        const long long nf = (long long)(G.ixmax - 1) * (G.jymax - 1) * (G.kzmax - 1);
+        const long long q = ((long long)i * (G.jymax - 1) + j) * (G.kzmax - 1) + k;
+#pragma unroll
+        for (int m = 0; m < 9; m++) F[m * nf + q] = Fo[m];
+    } else {
+        const long long q = cidx(G, i, j, k);
+#pragma unroll
+        for (int m = 0; m < 9; m++) F[m * G.nc + q] = Fo[m];
+    }
+}
+
+/* Faces along r (DIR 0) or phi (DIR 1), one thread marching over a run of MR
+ * consecutive faces f of one (j,k) or (i,k) line.  Face f takes the left slot
+ * of cell f and the right slot of cell f+1 (1 <= f <= N-1, N = nmax-2), so
+ * each step reconstructs cell f+1 once, both slots (cell_slots), uses its
+ * right slot now and carries its left slot to face f+1: one cell pass per
+ * face where flux_kernel makes two slot passes.  The first and last face of
+ * the direction keep flux_face (their periodic / free / fixed fills); a run
+ * starts with the left slot of its first interior cell.  Whole blocks share
+ * the run, so the edge faces never diverge inside a warp.  Same operations
+ * per state as flux_kernel, so the plain form keeps its bits. */
+template <typename T, int DIR, int MR, bool REFLAYOUT>
+__global__ void __launch_bounds__(128)
+march_flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
+                  T *__restrict__ F, Box b)
+{
+    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (DIR == 0 ? b.j0 : b.i0) + blockIdx.y * blockDim.y + threadIdx.y;
+    int f0 = (DIR == 0 ? b.i0 : b.j0) + blockIdx.z * MR;
+    const int fe = min(f0 + MR, DIR == 0 ? b.i1 : b.j1);
+    if (k >= b.k1 || t >= (DIR == 0 ? b.j1 : b.i1)) return;
+    const int N = (DIR == 0 ? G.ixmax : G.jymax) - 2;
+    const T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
+    if (f0 == 0) {
+        flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, DIR == 0 ? 0 : t, DIR == 0 ? t : 0, k);
+        f0 = 1;
+    }
+    const int fi = min(fe, N);   /* interior faces f0 .. fi-1 */
+    if (f0 < fi) {
+        T Lc[9];
+        slot_of<T, DIR, true>(G, V, f0, DIR == 0 ? f0 : t, DIR == 0 ? t : f0, k, dt, psicoef, Lc);
+#pragma unroll 1
+        for (int f = f0; f < fi; f++) {
+            const int i = DIR == 0 ? f : t, j = DIR == 0 ? t : f;
+            T Wl[9], R[9], Fo[9];
+            if (DIR == 0) cell_slots<T, 0>(G, V, f + 1, j, k, dt, psicoef, Wl, R);
+            else cell_slots<T, 1>(G, V, i, f + 1, k, dt, psicoef, Wl, R);
+            face_flux<T, DIR>(G, Lc, R, i, ch, Fo);
+            store_face<T, REFLAYOUT>(G, F, i, j, k, Fo);
+#pragma unroll
+            for (int m = 0; m < 9; m++) Lc[m] = Wl[m];
+        }
+    }
+    if (fe > N) flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, DIR == 0 ? N : t, DIR == 0 ? t : N, k);
 }
 
 /* The two z boundary faces of each (i,j) column (face 0 and face kzmax-2,
@@ -743,14 +809,22 @@ cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, co
         if (b.k1 <= b.k0) return cudaSuccess;
     }
     dim3 gr, bl;
-    grid3(b.k1 - b.k0, b.j1 - b.j0, b.i1 - b.i0, gr, bl);
-#define MHD_FLUX_CASE(D, RL) flux_kernel<T, D, RL><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b)
-    if (reflayout) {
-        if (dir == 0) MHD_FLUX_CASE(0, true); else if (dir == 1) MHD_FLUX_CASE(1, true); else MHD_FLUX_CASE(2, true);
-    } else {
-        if (dir == 0) MHD_FLUX_CASE(0, false); else if (dir == 1) MHD_FLUX_CASE(1, false); else MHD_FLUX_CASE(2, false);
+    if (dir < 2) {
+        /* r / phi faces marched in runs of MHD_MARCH_RUN along their direction */
+        const int nf = dir == 0 ? b.i1 - b.i0 : b.j1 - b.j0;
+        grid3(b.k1 - b.k0, dir == 0 ? b.j1 - b.j0 : b.i1 - b.i0, (nf + MHD_MARCH_RUN - 1) / MHD_MARCH_RUN, gr, bl);
+#define MHD_MARCH_CASE(D, RL) march_flux_kernel<T, D, MHD_MARCH_RUN, RL><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b)
+        if (reflayout) {
+            if (dir == 0) MHD_MARCH_CASE(0, true); else MHD_MARCH_CASE(1, true);
+        } else {
+            if (dir == 0) MHD_MARCH_CASE(0, false); else MHD_MARCH_CASE(1, false);
+        }
+#undef MHD_MARCH_CASE
+        return cudaGetLastError();
     }
-#undef MHD_FLUX_CASE
+    grid3(b.k1 - b.k0, b.j1 - b.j0, b.i1 - b.i0, gr, bl);
+    if (reflayout) flux_kernel<T, 2, true><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b);
+    else flux_kernel<T, 2, false><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b);
     return cudaGetLastError();
 }
 

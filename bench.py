@@ -570,8 +570,12 @@ def main():
         Vh = np.ascontiguousarray(V.copy())
         M.pin(Uh)
         M.pin(Vh)
-        d32.timer_start()
         t = 0.0
+        for _ in range(args.warmup):                     # untimed, like the resident form
+            d32.upload_state(Uh, Vh)
+            rc, t, dt, ch, cnt = d32.step(t)
+            d32.download_into(Uh, Vh)
+        d32.timer_start()
         for _ in range(args.steps):
             d32.upload_state(Uh, Vh)
             rc, t, dt, ch, cnt = d32.step(t)
