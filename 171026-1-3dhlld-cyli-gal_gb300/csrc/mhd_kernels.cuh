@@ -6,8 +6,10 @@
  * One RK stage = flux(r) + flux(phi) + flux(z: boundary faces, interior
  * faces) + update + ghost (the default), or flux(r) + flux(phi) + z fluxes
  * fused into the update + ghost, or the fused stage kernel + ghost:
- *   flux    one thread per face the update reads; reconstruction of the two
- *           adjacent cells, Riemann solver, GLM flux -> F/G/H[9][cells]
+ *   flux    every face the update reads: reconstruction (each cell once, both
+ *           slots, shared along the direction by a marching thread in r and
+ *           phi and by warp shuffles in z), Riemann solver, GLM flux ->
+ *           F/G/H[9][cells]
  *   update  one thread per interior cell: sources, the stage's conservative
  *           update, and -- because everything after it up to the next stage
  *           is pointwise for interior cells -- the k=1 v_z zeroing (RK2), the
@@ -25,7 +27,7 @@
 
 /* faces per thread of the marched r and phi flux kernels */
 #ifndef MHD_MARCH_RUN
-#define MHD_MARCH_RUN 8
+#define MHD_MARCH_RUN 16
 #endif
 
 namespace mhd {
@@ -55,18 +57,6 @@ __device__ __forceinline__ void flux_face(const Geom &G, const T *__restrict__ V
     }
 }
 
-template <typename T, int DIR, bool REFLAYOUT>
-__global__ void __launch_bounds__(128)
-flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
-            T *__restrict__ F, Box b)
-{
-    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = b.j0 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = b.i0 + blockIdx.z;
-    if (k >= b.k1 || j >= b.j1) return;
-    flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, i, j, k);
-}
-
 /* one face's flux into F (cell layout) or the reference's face layout */
 template <typename T, bool REFLAYOUT>
 __device__ __forceinline__ void store_face(const Geom &G, T *__restrict__ F, int i, int j, int k, const T Fo[9])
@@ -88,11 +78,11 @@ __device__ __forceinline__ void store_face(const Geom &G, T *__restrict__ F, int
  * of cell f and the right slot of cell f+1 (1 <= f <= N-1, N = nmax-2), so
  * each step reconstructs cell f+1 once, both slots (cell_slots), uses its
  * right slot now and carries its left slot to face f+1: one cell pass per
- * face where flux_kernel makes two slot passes.  The first and last face of
- * the direction keep flux_face (their periodic / free / fixed fills); a run
- * starts with the left slot of its first interior cell.  Whole blocks share
+ * face where a thread per face (flux_face) makes two slot passes.  The first
+ * and last face of the direction keep flux_face (their periodic / free /
+ * fixed fills); a run starts with the left slot of its first interior cell.  Whole blocks share
  * the run, so the edge faces never diverge inside a warp.  Same operations
- * per state as flux_kernel, so the plain form keeps its bits. */
+ * per state as face_states, so the plain form keeps its bits. */
 template <typename T, int DIR, int MR, bool REFLAYOUT>
 __global__ void __launch_bounds__(128)
 march_flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
@@ -128,10 +118,58 @@ march_flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, 
     if (fe > N) flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, DIR == 0 ? N : t, DIR == 0 ? t : N, k);
 }
 
+/* Interior z faces (1 .. kzmax-3 within the box), one warp walking each
+ * (i,j) row in chunks of 32 cells: lane l reconstructs cell c = c0 + l once,
+ * both slots (cell_slots), and forms face c-1 from its own right slot and the
+ * left slot of cell c-1, which the lane below holds (a shuffle; lane 0 takes
+ * lane 31's from the previous chunk).  One cell pass per face where the
+ * four-cell stencil of interior_states makes two slot passes; loads stay
+ * coalesced along k.  Same operations per state as face_states, so the
+ * plain form keeps its bits.  FP32: held to 64 registers (8 blocks per SM),
+ * 1.48 against 1.56 ms at 78 registers for 512x512x256. */
+template <typename T, bool REFLAYOUT>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1)
+zwalk_flux_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc, T *__restrict__ F, Box b)
+{
+    const int lane = threadIdx.x & 31;
+    const int nj = b.j1 - b.j0;
+    const long long nrow = (long long)(b.i1 - b.i0) * nj;
+    const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= nrow) return;   /* a whole warp */
+    const int i = b.i0 + (int)(row / nj), j = b.j0 + (int)(row % nj);
+    const int flo = max(b.k0, 1), fhi = min(b.k1, G.kzmax - 2);   /* faces flo .. fhi-1, cells flo .. fhi */
+    const T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
+    T carry[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) carry[m] = T(0.0);
+#pragma unroll 1
+    for (int c0 = flo; c0 <= fhi; c0 += 32) {   /* warp-uniform */
+        const int c = c0 + lane;
+        const bool live = c <= fhi;
+        T Wl[9], Wr[9], L[9];
+        if (live) cell_slots<T, 2>(G, V, i, j, c, dt, psicoef, Wl, Wr);
+        else {
+#pragma unroll
+            for (int m = 0; m < 9; m++) { Wl[m] = T(0.0); Wr[m] = T(0.0); }
+        }
+#pragma unroll
+        for (int m = 0; m < 9; m++) {
+            const T up = __shfl_up_sync(0xffffffffu, Wl[m], 1);
+            L[m] = lane == 0 ? carry[m] : up;
+            carry[m] = __shfl_sync(0xffffffffu, Wl[m], 31);
+        }
+        if (live && c > flo) {
+            T Fo[9];
+            face_flux<T, 2>(G, L, Wr, i, ch, Fo);
+            store_face<T, REFLAYOUT>(G, F, i, j, c - 1, Fo);
+        }
+    }
+}
+
 /* The two z boundary faces of each (i,j) column (face 0 and face kzmax-2,
  * which take the special left/right states of face_states), one thread per
  * face with the side slowest so every warp takes one branch; the interior
- * z faces run in flux_kernel<T,2> without that divergence. */
+ * z faces run in zwalk_flux_kernel without that divergence. */
 template <typename T, bool REFLAYOUT>
 __global__ void __launch_bounds__(128)
 flux_zedge_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
@@ -314,7 +352,7 @@ __device__ __forceinline__ void face_flux_at(const Geom &G, const T *__restrict_
  * once and kept in shared memory, so no chunk diverges on them.  Each lane
  * then updates its cell from the r and phi fluxes in F, G and its z fluxes in
  * registers: the z fluxes never reach HBM and the update's loads overlap other
- * warps' flux arithmetic.  Same operations as flux_kernel<T,2> followed by
+ * warps' flux arithmetic.  Same operations as the split z flux followed by
  * update_kernel<T>, so the plain form keeps its bits.  Measured at
  * 512x512x256 (FP32): 6.3 ms against 1.9 + 3.4 ms for the two kernels apart
  * (at 128 registers 8.5 ms, 80 registers 6.8 ms; an L2 prefetch of each
@@ -822,9 +860,10 @@ cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, co
 #undef MHD_MARCH_CASE
         return cudaGetLastError();
     }
-    grid3(b.k1 - b.k0, b.j1 - b.j0, b.i1 - b.i0, gr, bl);
-    if (reflayout) flux_kernel<T, 2, true><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b);
-    else flux_kernel<T, 2, false><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b);
+    /* interior z faces: one warp per (i,j) row, four rows per block */
+    const long long nrow = (long long)(b.i1 - b.i0) * (b.j1 - b.j0);
+    if (reflayout) zwalk_flux_kernel<T, true><<<nblocks(nrow, 4), 128, 0, st>>>(G, V, sc, F, b);
+    else zwalk_flux_kernel<T, false><<<nblocks(nrow, 4), 128, 0, st>>>(G, V, sc, F, b);
     return cudaGetLastError();
 }
 
