@@ -812,6 +812,10 @@ static int batch_run(mhd_batch *b, int nsteps, double *t, int *status)
         t[d] = b->ctx[d]->h_sc->t;
         b->ctx[d]->vcur = b->parity;
         if (b->ctx[d]->h_sc->dtbad) b->stopped[d] = 1;
+        if (b->ctx[d]->h_sc->err) {   /* a disc's staged update tile gave up waiting (disc-graph mode) */
+            herr = 1;
+            b->ctx[d]->h_sc->err = 0;
+        }
     }
     if (status)
         for (int d = 0; d < n; d++) status[d] = b->stopped[d] ? MHD_ERR_DT : MHD_OK;

@@ -193,6 +193,50 @@ static void free_all(mhd_ctx *ctx)
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->st_aux) { cudaStreamSynchronize(ctx->st_aux); cudaStreamDestroy(ctx->st_aux); }
     if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx->maps;
+}
+
+/* Tensor maps for the TMA-staged update: each FP32 array viewed as a 2D tensor
+ * [nvar][nc] (row stride nc * 4 bytes, a multiple of 16 only when nc % 4 == 0;
+ * tile coordinates are 32-bit).  cuTensorMapEncodeTiled comes from the driver
+ * through the runtime's entry-point query, so the library links no driver
+ * library.  NULL when the layout or the driver does not allow it. */
+typedef CUresult (*encode_tiled_fn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static UpdMaps *make_upd_maps(mhd_ctx *ctx)
+{
+    if (!ctx->fp32 || ctx->nc % 4 != 0 || ctx->nc + 2 * MHD_UPD_TILE >= (1LL << 31)) return NULL;
+    void *fn = NULL;
+    cudaDriverEntryPointQueryResult qr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) != cudaSuccess ||
+        qr != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return NULL;
+    }
+    encode_tiled_fn enc = (encode_tiled_fn)fn;
+    UpdMaps *m = new (std::nothrow) UpdMaps;
+    if (!m) return NULL;
+    auto mk = [&](CUtensorMap *t, void *base, int nvar, int box) {
+        cuuint64_t dims[2] = {(cuuint64_t)ctx->nc, (cuuint64_t)nvar};
+        cuuint64_t strides[1] = {(cuuint64_t)ctx->nc * sizeof(float)};
+        cuuint32_t boxd[2] = {(cuuint32_t)box, (cuuint32_t)nvar};
+        cuuint32_t es[2] = {1, 1};
+        return enc(t, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, boxd, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    const int T = MHD_UPD_TILE, W = MHD_UPD_WIDE;
+    bool ok = mk(&m->v[0], ctx->Va, 9, T) && mk(&m->v[1], ctx->Vb, 9, T) && mk(&m->f, ctx->F, 9, T) &&
+              mk(&m->g, ctx->Gf, 9, T) && mk(&m->un, ctx->U, 9, T) && mk(&m->u1, ctx->U1, 9, T) &&
+              mk(&m->fm, ctx->F, 9, W) && mk(&m->gm, ctx->Gf, 9, W) && mk(&m->h, ctx->H, 9, W) &&
+              mk(&m->rho, ctx->rhofloor, 1, T);
+    if (!ok) {
+        delete m;
+        return NULL;
+    }
+    return m;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -378,6 +422,8 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     CKC(cudaMallocHost((void **)&ctx->h_part, ctx->npart * sizeof(MaxLoc)));
     CKC(cudaMalloc((void **)&ctx->d_cnt, 3 * 3 * sizeof(int)));
     CKC(cudaMallocHost((void **)&ctx->h_cnt, 3 * 3 * sizeof(int)));
+    ctx->maps = make_upd_maps(ctx);
+    ctx->upd_tma = 0;
     ctx->stage_n = 1LL << 24;
     if (ctx->fp32) {
         CKC(cudaMalloc((void **)&ctx->d_stage, NSTAGE * ctx->stage_n * sizeof(double)));
@@ -619,7 +665,10 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
         CK(cudaEventRecord(ctx->ev_join, ctx->st_aux));
         LAUNCH(PK_FLUX_Z, launch_flux_zinterior(ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), ctx->st));
         CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
-        LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
+        if (ctx->upd_tma)
+            LAUNCH(PK_UPDATE, launch_update_tma(ctx->G, a, *ctx->maps, ctx->vcur, &ctx->d_sc->err, ctx->st));
+        else
+            LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
     }
     LAUNCH(PK_GHOST, launch_ghost(ctx->G, a, ctx->st));
     ctx->vcur ^= 1;
@@ -657,7 +706,12 @@ extern "C" int mhd_tvdrk(mhd_ctx *ctx, double dt, double ch, int counters[3])
     int rc = run_stages(ctx, ctx->d_cnt);
     if (rc) return rc;
     CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, 9 * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(&h->err, &ctx->d_sc->err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    if (h->err) {   /* a staged tile's copies did not land: that tile was left as it was */
+        h->err = 0;
+        return MHD_ERR_TIMEOUT;
+    }
     int last = ctx->p.scheme == MHD_SCHEME_RK2 ? 1 : 2;
     if (counters) for (int c = 0; c < 3; c++) counters[c] = ctx->h_cnt[3 * last + c];
     return MHD_OK;
@@ -917,6 +971,10 @@ extern "C" int mhd_run(mhd_ctx *ctx, int nsteps, double *t)
     CK(cudaMemcpyAsync(h, ctx->d_sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     *t = h->t;
+    if (h->err) {
+        h->err = 0;
+        return MHD_ERR_TIMEOUT;
+    }
     return h->dtbad ? MHD_ERR_DT : MHD_OK;
 }
 
@@ -1075,6 +1133,25 @@ extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
         ctx->graph_ready = 0;
     }
     return MHD_OK;
+}
+
+extern "C" int mhd_set_update_path(mhd_ctx *ctx, int tma)
+{
+    if (!ctx || tma < 0 || tma > 1 || (tma && !ctx->maps)) return MHD_ERR_ARG;
+    ctx->upd_tma = tma;
+    if (ctx->graph_ready) {
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int q = 0; q < 2; q++)
+            if (ctx->gexecs[q]) { cudaGraphExecDestroy(ctx->gexecs[q]); ctx->gexecs[q] = NULL; }
+        ctx->graph_ready = 0;
+    }
+    return MHD_OK;
+}
+
+extern "C" int mhd_update_path(const mhd_ctx *ctx)
+{
+    if (!ctx) return MHD_ERR_ARG;
+    return ctx->upd_tma;
 }
 
 extern "C" int mhd_prof_read(mhd_ctx *ctx, double *ms, long long *launches)

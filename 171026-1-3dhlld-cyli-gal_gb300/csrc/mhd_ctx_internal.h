@@ -33,6 +33,10 @@ struct mhd_ctx {
     /* stage shape: fused = one kernel for fluxes + update (else the four
      * separate kernels), tile height tj (j) and run length seg (i) */
     int fused, stage_tj, stage_seg;
+    /* tensor maps of the TMA-staged update (precision form, when the layout
+     * allows it; else NULL) and whether the split stage uses it */
+    mhd::UpdMaps *maps;
+    int upd_tma;
     mhd::StepScalars *d_sc, *h_sc;
     double *d_trig, *h_trig;
     float *d_trigf;

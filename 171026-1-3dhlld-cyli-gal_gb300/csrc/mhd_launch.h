@@ -6,7 +6,14 @@
 #ifndef MHD_LAUNCH_H
 #define MHD_LAUNCH_H
 
+#include <cuda.h>   /* CUtensorMap (a type only: the library does not link the driver API) */
+
 #include "mhd_dev.cuh"
+
+/* cells per tile of the TMA-staged update, and the width of its windows that
+ * start up to 3 cells before the tile (TMA rows start on 16-byte boundaries) */
+#define MHD_UPD_TILE 128
+#define MHD_UPD_WIDE 136
 
 namespace mhd {
 
@@ -18,6 +25,15 @@ struct Box {
 struct MaxLoc {
     double v;
     long long q;
+};
+
+/* Tensor maps of the arrays the TMA-staged update reads (precision form),
+ * each array viewed as a 2D FP32 tensor [nvar][nc] with row stride nc */
+struct UpdMaps {
+    CUtensorMap v[2];          /* Va, Vb: box {MHD_UPD_TILE, 9} */
+    CUtensorMap f, g, un, u1;  /* F, G, U, U1: box {MHD_UPD_TILE, 9} */
+    CUtensorMap fm, gm, h;     /* F, G, H: box {MHD_UPD_WIDE, 9} */
+    CUtensorMap rho;           /* rhofloor: box {MHD_UPD_TILE, 1} */
 };
 
 template <typename T>
@@ -45,6 +61,8 @@ struct StageArgs {
     cudaError_t launch_zedge(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, Box b,  \
                              cudaStream_t st);                                                               \
     cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                        \
+    cudaError_t launch_update_tma(const Geom &G, const StageArgs<T> &a, const UpdMaps &maps, int vpar,      \
+                                  int *err, cudaStream_t st); /* precision form only */                    \
     cudaError_t launch_ghost(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                         \
     cudaError_t launch_stage(const Geom &G, const StageArgs<T> &a, int tj, int seg, cudaStream_t st);        \
     cudaError_t prepare_stage(T *); /* shared-memory attribute of the fused kernels */                       \

@@ -133,6 +133,8 @@ def lib():
         "mhd_upload_state": (C.c_int, [vp, vp, vp]),
         "mhd_prof_enable": (C.c_int, [vp, C.c_int]),
         "mhd_set_stage_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+        "mhd_set_update_path": (C.c_int, [vp, C.c_int]),
+        "mhd_update_path": (C.c_int, [vp]),
         "mhd_prof_read": (C.c_int, [vp, DP, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]),
         "mhd_launch_count": (C.c_longlong, [vp]),
         "mhd_timer_start": (C.c_int, [vp]),
@@ -480,6 +482,14 @@ class Disc:
         j-cells per tile, seg r-cells per run), 2 z fluxes fused into the
         update (mhd_set_stage_shape)."""
         check(lib().mhd_set_stage_shape(self.h, int(fused), int(tj), int(seg)), "mhd_set_stage_shape")
+
+    def set_update_path(self, tma):
+        """1: the split stage's update stages its tiles in shared memory with
+        tensor copies; 0: thread-by-thread loads (mhd_set_update_path)."""
+        check(lib().mhd_set_update_path(self.h, int(tma)), "mhd_set_update_path")
+
+    def update_path(self):
+        return int(lib().mhd_update_path(self.h))
 
     def launches(self):
         return int(lib().mhd_launch_count(self.h))

@@ -247,6 +247,15 @@ int mhd_prof_read(mhd_ctx *ctx, double ms[MHD_PROF_NKIND], long long launches[MH
  * (tile 32 k-cells x tj j-cells, tj = 7, marching over runs of seg cells in
  * r).  All give the same bits in the plain form. */
 int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg);
+/* How the split stage's update reads its inputs (precision form): tma = 0
+ * (the default) loads them thread by thread; tma = 1 stages each tile of 128
+ * cells in shared memory with tensor copies, where the layout allows it
+ * (cells per variable a multiple of 4).  MHD_ERR_ARG for tma = 1 where it is
+ * not available (plain form, other layouts).  A tile whose copies do not
+ * land within a bounded wait makes the step return MHD_ERR_TIMEOUT. */
+int mhd_set_update_path(mhd_ctx *ctx, int tma);
+/* 1 if the split stage's update is TMA-staged, 0 if not. */
+int mhd_update_path(const mhd_ctx *ctx);
 /* Kernels this context has launched since creation. */
 long long mhd_launch_count(const mhd_ctx *ctx);
 /* Stream timer: start synchronises the stream and records an event; stop
