@@ -937,6 +937,21 @@ __global__ void source_kernel(Geom G, const T *__restrict__ V, const StepScalars
 /* ------------------------------------------------------------------------ */
 static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+/* SMs of the current device (152 on GB300), read once */
+static inline int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            n = v;
+        else
+            n = 152;
+    }
+    return n;
+}
+
 /* 128-thread blocks laid along k (fastest index), rows of j stacked when the
  * k extent is short; one grid z-slice per i */
 static inline void grid3(int nk, int nj, int ni, dim3 &grid, dim3 &block)
@@ -989,14 +1004,24 @@ cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, co
     }
     dim3 gr, bl;
     if (dir < 2) {
-        /* r / phi faces marched in runs of MHD_MARCH_RUN along their direction */
+        /* r / phi faces marched in runs along their direction: MHD_MARCH_RUN
+         * faces per thread where that still gives every SM several blocks,
+         * shorter runs on small grids */
         const int nf = dir == 0 ? b.i1 - b.i0 : b.j1 - b.j0;
-        grid3(b.k1 - b.k0, dir == 0 ? b.j1 - b.j0 : b.i1 - b.i0, (nf + MHD_MARCH_RUN - 1) / MHD_MARCH_RUN, gr, bl);
-#define MHD_MARCH_CASE(D, RL) march_flux_kernel<T, D, MHD_MARCH_RUN, RL><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b)
+        const long long lines = (long long)(b.k1 - b.k0) * (dir == 0 ? b.j1 - b.j0 : b.i1 - b.i0);
+        const long long want = 4LL * 128 * sm_count();
+        const int mr = reflayout || lines * ((nf + MHD_MARCH_RUN - 1) / MHD_MARCH_RUN) >= want ? MHD_MARCH_RUN
+                       : lines * ((nf + 3) / 4) >= want ? 4 : 1;
+        grid3(b.k1 - b.k0, dir == 0 ? b.j1 - b.j0 : b.i1 - b.i0, (nf + mr - 1) / mr, gr, bl);
+#define MHD_MARCH_CASE(D, MR, RL) march_flux_kernel<T, D, MR, RL><<<gr, bl, 0, st>>>(G, V, Vinit, sc, F, b)
         if (reflayout) {
-            if (dir == 0) MHD_MARCH_CASE(0, true); else MHD_MARCH_CASE(1, true);
+            if (dir == 0) MHD_MARCH_CASE(0, MHD_MARCH_RUN, true); else MHD_MARCH_CASE(1, MHD_MARCH_RUN, true);
+        } else if (mr == MHD_MARCH_RUN) {
+            if (dir == 0) MHD_MARCH_CASE(0, MHD_MARCH_RUN, false); else MHD_MARCH_CASE(1, MHD_MARCH_RUN, false);
+        } else if (mr == 4) {
+            if (dir == 0) MHD_MARCH_CASE(0, 4, false); else MHD_MARCH_CASE(1, 4, false);
         } else {
-            if (dir == 0) MHD_MARCH_CASE(0, false); else MHD_MARCH_CASE(1, false);
+            if (dir == 0) MHD_MARCH_CASE(0, 1, false); else MHD_MARCH_CASE(1, 1, false);
         }
 #undef MHD_MARCH_CASE
         return cudaGetLastError();
