@@ -647,6 +647,7 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     a.Vout = (T *)vnext_ptr(ctx); a.Uraw = (T *)ctx->Uraw;
     a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.trigf = ctx->d_trigf; a.kind = kind; a.last = last; a.counters = counters;
     a.Vinit = Vinit;
+    a.zghost = ctx->fused == 0;   /* the split update fills the interior columns' k-plane ghosts */
     if (ctx->fused == 1) {
         LAUNCH(PK_STAGE, launch_stage(ctx->G, a, ctx->stage_tj, ctx->stage_seg, ctx->st));
     } else if (ctx->fused == 2) {

@@ -258,6 +258,42 @@ __device__ __forceinline__ T flux_div(const T g[6], T fu, T fl, T gu, T gl, T hu
     return ((g[1] * fu - g[0] * fl) + (g[3] * gu - g[2] * gl) + (g[5] * hu - g[4] * hl));
 }
 
+/* The k-plane ghost an interior cell (i,j,k) is the source of, if any (the
+ * z fills: RK2 ZLeftVzAntisym / ZRightFree, k=0 <- k=2 with rho v_z negated
+ * and kzmax-1 <- kzmax-2, zboundary.h:67-96,203-226; RK3 periodic, k=0 <-
+ * kzmax-2 and kzmax-1 <- 1, zboundary.h:105-161), filled from the cell's raw
+ * updated state u with the ghost's own pointwise tail -- the operations of
+ * ghost_cell for that ghost, done while the source's row is in flight, so the
+ * ghost kernel leaves these uncoalesced cells out.  Floor counts go straight
+ * to the counters. */
+template <typename T>
+__device__ __forceinline__ void zghost_fill(const Geom &G, const StageArgs<T> &a, int i, int j, int k, const T u[9])
+{
+    int kg;
+    bool flip = false;
+    if (G.scheme == MHD_SCHEME_RK2) {
+        if (k == 2) { kg = 0; flip = true; }
+        else if (k == G.kzmax - 2) kg = G.kzmax - 1;
+        else return;
+    } else {
+        if (k == G.kzmax - 2) kg = 0;
+        else if (k == 1) kg = G.kzmax - 1;
+        else return;
+    }
+    const long long nc = G.nc, qg = cidx(G, i, j, kg);
+    T ug[9], W[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) ug[m] = (flip && m == 3) ? -u[m] : u[m];
+    if (a.last) absorb<T>(G, a.Uinit, i, j, kg, G.scheme == MHD_SCHEME_RK2, ug);
+    const int flags = utov_check<T>(G, i, a.rhofloor[qg], ug, W);
+    T *Uo = (a.kind == 0 || a.kind == 1) ? a.U1 : a.Un;
+#pragma unroll
+    for (int m = 0; m < 9; m++) { Uo[m * nc + qg] = ug[m]; a.Vout[m * nc + qg] = W[m]; }
+    if (flags & 1) atomicAdd(&a.counters[0], 1);
+    if (flags & 2) atomicAdd(&a.counters[1], 1);
+    if (flags & 4) atomicAdd(&a.counters[2], 1);
+}
+
 /* a cell's stage inputs read from global memory: V, U^n, U^(k), the floor */
 template <typename T>
 struct GmemCell {
@@ -300,6 +336,7 @@ __device__ __forceinline__ int update_core(const Geom &G, const StageArgs<T> &a,
     if (is_bc_source(G, i, j, k)) {
 #pragma unroll
         for (int m = 0; m < 9; m++) a.Uraw[m * nc + q] = u[m];
+        if (a.zghost) zghost_fill<T>(G, a, i, j, k, u);
     }
     if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);   /* zboundary.h:87 */
     if (a.last) absorb<T>(G, a.Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
@@ -730,22 +767,36 @@ __device__ __forceinline__ void ghost_source(const Geom &G, int i, int j, int k,
 }
 
 /* number of ghost cells and the ghost cell with enumeration index tid:
- * k planes (k=0, kzmax-1), then j planes, then i planes */
-__device__ __forceinline__ unsigned ghost_count(const Geom &G)
+ * k planes (k=0, kzmax-1), then j planes, then i planes.  zg = 1: of the k
+ * planes only the rim (i or j a ghost index); the update fills the rest */
+__host__ __device__ __forceinline__ unsigned ghost_kplane(unsigned ni, unsigned nj, int zg)
 {
-    const unsigned nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
-    return 2 * ni * nj + 2 * ni * (nk - 2) + 2 * (nj - 2) * (nk - 2);
+    return zg ? 2 * nj + 2 * (ni - 2) : ni * nj;
 }
 
-__device__ __forceinline__ void ghost_cell_of(const Geom &G, unsigned tid, int &i, int &j, int &k)
+__host__ __device__ __forceinline__ unsigned ghost_count(const Geom &G, int zg = 0)
 {
     const unsigned nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
-    const unsigned nkplane = 2 * ni * nj;
+    return 2 * ghost_kplane(ni, nj, zg) + 2 * ni * (nk - 2) + 2 * (nj - 2) * (nk - 2);
+}
+
+__device__ __forceinline__ void ghost_cell_of(const Geom &G, unsigned tid, int zg, int &i, int &j, int &k)
+{
+    const unsigned nk = G.kzmax, nj = G.jymax, ni = G.ixmax;
+    const unsigned kp = ghost_kplane(ni, nj, zg);
+    const unsigned nkplane = 2 * kp;
     const unsigned njplane = 2 * ni * (nk - 2);
     if (tid < nkplane) {
-        k = (tid < ni * nj) ? 0 : (int)nk - 1;
-        unsigned r = tid % (ni * nj);
-        i = (int)(r / nj); j = (int)(r % nj);
+        k = (tid < kp) ? 0 : (int)nk - 1;
+        unsigned r = tid % kp;
+        if (!zg) {
+            i = (int)(r / nj); j = (int)(r % nj);
+        } else if (r < 2 * nj) {
+            i = (r < nj) ? 0 : (int)ni - 1; j = (int)(r % nj);
+        } else {
+            r -= 2 * nj;
+            j = (r < ni - 2) ? 0 : (int)nj - 1; i = 1 + (int)(r % (ni - 2));
+        }
     } else if (tid < nkplane + njplane) {
         unsigned r = tid - nkplane;
         j = (r < ni * (nk - 2)) ? 0 : (int)nj - 1;
@@ -763,7 +814,7 @@ template <typename T>
 __device__ __forceinline__ int ghost_cell(const Geom &G, const StageArgs<T> &a, unsigned tid)
 {
     int i, j, k;
-    ghost_cell_of(G, tid, i, j, k);
+    ghost_cell_of(G, tid, a.zghost, i, j, k);
     int si, sj, sk;
     unsigned neg;
     ghost_source(G, i, j, k, si, sj, sk, neg);
@@ -789,7 +840,7 @@ __global__ void __launch_bounds__(128) ghost_kernel(Geom G, StageArgs<T> a)
     if (a.sc->dtbad) return;
     const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
     int flags = 0;
-    if (tid < ghost_count(G)) flags = ghost_cell<T>(G, a, tid);
+    if (tid < ghost_count(G, a.zghost)) flags = ghost_cell<T>(G, a, tid);
     add_counters(flags, a.counters);
 }
 
@@ -1116,7 +1167,7 @@ cudaError_t launch_zupdate_t(const Geom &G, const StageArgs<T> &a, cudaStream_t 
 template <typename T>
 cudaError_t launch_ghost_t(const Geom &G, const StageArgs<T> &a, cudaStream_t st)
 {
-    long long ng = 2LL * G.ixmax * G.jymax + 2LL * G.ixmax * (G.kzmax - 2) + 2LL * (G.jymax - 2) * (G.kzmax - 2);
+    const long long ng = ghost_count(G, a.zghost);
     ghost_kernel<T><<<nblocks(ng, 128), 128, 0, st>>>(G, a);
     return cudaGetLastError();
 }

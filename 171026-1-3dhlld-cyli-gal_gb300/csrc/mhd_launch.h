@@ -49,6 +49,7 @@ struct StageArgs {
     int kind, last;
     int *counters;
     const T *Vinit;        /* initial primitives (z MC boundary states; fused stage) */
+    int zghost = 0;        /* 1: the update fills the k-plane ghosts of interior (i,j) columns */
 };
 
 #define MHD_DECLARE_LAUNCHERS(T)                                                                             \
