@@ -182,7 +182,6 @@ static void free_all(mhd_ctx *ctx)
     if (ctx->h_trig) cudaFreeHost(ctx->h_trig);
     if (ctx->h_part) cudaFreeHost(ctx->h_part);
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
-    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     for (int q = 0; q < 2; q++)
         if (ctx->gexecs[q]) cudaGraphExecDestroy(ctx->gexecs[q]);
     for (int q = 0; q < 2 * MAXSLOT; q++)

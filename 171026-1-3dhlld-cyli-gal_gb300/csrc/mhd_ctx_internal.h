@@ -51,8 +51,7 @@ struct mhd_ctx {
     double omdiff;
     int uploaded;
     cudaError_t last_cuda;
-    /* mhd_run graph */
-    cudaGraphExec_t gexec;
+    /* mhd_run step graphs, one per starting primitive parity */
     cudaGraphExec_t gexecs[2];
     int graph_ready, graph_launches;
     int *d_cnt_run;
