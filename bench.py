@@ -437,11 +437,23 @@ def rank_info():
 
 
 def dist_init(world):
+    """One process per GPU under torchrun: a gloo group for the barrier and
+    the max-over-ranks timing only (the replicas exchange no data)."""
     if world <= 1:
         return None
     import torch.distributed as dist
     dist.init_process_group("gloo")
     return dist
+
+
+def max_over_ranks(dist, x):
+    """The largest of every rank's x (x itself on one process)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def main():
@@ -517,11 +529,7 @@ def main():
     # separate pass of the same steps through mhd_step, events around each launch
     d32.upload(U, V)
     _, _, _, kern, _ = time_steps(M, d32, max(3, min(args.steps, 5)), 1, prof=True)
-    if dist:
-        import torch
-        tt = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(dist, ms)
     value = zones * args.steps * world / (ms / 1e3)
 
     # dominant kernel and its roofline (algorithmic bytes, FP32 = 4 B per value)
@@ -578,13 +586,15 @@ def main():
         # each step timed on its own (the download returns with the result on
         # the host, so the steps are serial either way); the sum is the region
         step_ms = []
+        if dist:
+            dist.barrier()
         for _ in range(args.steps):
             d32.timer_start()
             d32.upload_state(Uh, Vh)
             rc, t, dt, ch, cnt = d32.step(t)
             d32.download_into(Uh, Vh)
             step_ms.append(d32.timer_stop())
-        ems = sum(step_ms)
+        ems = max_over_ranks(dist, sum(step_ms))
         M.pin(Uh, False)
         M.pin(Vh, False)
         nb = 2 * 9 * grid.ixmax * grid.jymax * grid.kzmax * 8
@@ -600,7 +610,10 @@ def main():
     p64 = with_precision(M, params, "fp64")
     d64 = M.Disc(grid, p64)
     d64.upload(U, V)
+    if dist:
+        dist.barrier()
     ms64, wall64, l64, kern64, _ = time_steps(M, d64, f64_steps, 1, prof=True)
+    ms64 = max_over_ranks(dist, ms64)
     d64.close()
     v64 = zones * f64_steps * world / (ms64 / 1e3)
 
