@@ -551,13 +551,13 @@ def main():
         "zupdate": zones * (64 - 9) * s,
     }
     achieved = per_launch.get(dom, 0) / (dms / dn / 1e3) / 1e9 if dn else None
-    # DRAM bytes (read + write) per zone per launch from ncu captures at
-    # 256x256x128 (profiles/split_stage_fp32_256x256x128.md), scaled here by the
-    # zones of this workload; the update figure is a first-stage launch (the
-    # other two stages also read U^(k))
-    measured_traffic = {"update": (1.613456e9 + 0.626855e9) / 8388608,
-                        "flux_r": (0.338613e9 + 0.269102e9) / 8388608,
-                        "flux_phi": (0.331223e9 + 0.268120e9) / 8388608}
+    # DRAM bytes (read + write) per zone per launch from the ncu capture of the
+    # first stage of a 256x256x128 step (the split-stage summary under
+    # profiles/), scaled here by the zones of this workload; the update figure
+    # is a first-stage launch (the other two stages also read U^(k))
+    measured_traffic = {"update": (1.613262e9 + 0.632994e9) / 8388608,
+                        "flux_r": (0.384357e9 + 0.262446e9) / 8388608,
+                        "flux_phi": (0.382199e9 + 0.262957e9) / 8388608}
     traffic = measured_traffic[dom] * zones if dom in measured_traffic else None
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
