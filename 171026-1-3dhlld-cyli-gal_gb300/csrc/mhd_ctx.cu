@@ -448,6 +448,34 @@ extern "C" void mhd_destroy(mhd_ctx *ctx)
 
 extern "C" void *mhd_stream(mhd_ctx *ctx) { return ctx ? (void *)ctx->st : NULL; }
 
+/* device selection for one-process-per-GPU launches: the ordinal is checked
+ * against the visible device count before cudaSetDevice */
+extern "C" int mhd_use_device(int ordinal)
+{
+    mhd_ctx *ctx = NULL;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return MHD_ERR_NODEV;
+    }
+    if (ordinal < 0 || ordinal >= ndev) return MHD_ERR_ARG;
+    CK(cudaSetDevice(ordinal));
+    return MHD_OK;
+}
+
+extern "C" int mhd_current_device(int *ordinal)
+{
+    mhd_ctx *ctx = NULL;
+    if (!ordinal) return MHD_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return MHD_ERR_NODEV;
+    }
+    CK(cudaGetDevice(ordinal));
+    return MHD_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* transfers                                                                 */
 /* ------------------------------------------------------------------------ */

@@ -106,6 +106,8 @@ def lib():
         "mhd_gdl_output_cylinder": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(MhdGrid), DP]),
         "mhd_checkpoint_begin": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_double]),
         "mhd_checkpoint_wait": (C.c_int, [vp]),
+        "mhd_use_device": (C.c_int, [C.c_int]),
+        "mhd_current_device": (C.c_int, [C.POINTER(C.c_int)]),
         "mhd_create": (C.c_int, [C.POINTER(MhdGrid), C.POINTER(MhdParams), C.POINTER(vp)]),
         "mhd_destroy": (None, [vp]),
         "mhd_upload": (C.c_int, [vp, vp, vp, vp, vp, vp]),
@@ -364,6 +366,18 @@ def restart(root, nout, tint, grid, params):
     check(lib().mhd_restart(_path(root), int(nout), float(tint), C.byref(grid.g), C.byref(params),
                             U, V, Ui, Vi, rf, C.byref(t), C.byref(tout)), "mhd_restart")
     return U, V, Ui, Vi, rf, t.value, tout.value
+
+
+def use_device(ordinal):
+    """Make CUDA device `ordinal` current for this thread (mhd_use_device):
+    one process per GPU calls it with its local rank before any context."""
+    check(lib().mhd_use_device(int(ordinal)), "mhd_use_device")
+
+
+def current_device():
+    d = C.c_int(-1)
+    check(lib().mhd_current_device(C.byref(d)), "mhd_current_device")
+    return d.value
 
 
 class Disc:

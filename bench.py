@@ -8,17 +8,21 @@ reduction, dt guard, three stages.
 
 * ``value``     the FP32 + FP64-repair form, state resident in HBM.
 * ``fp64``      the plain FP64 form (bit-identical to the reference C), same
-                workload, fewer steps.
+                workload, fewer steps; its own per-kernel times and an
+                end-to-end figure through the C-ABI.
 * ``e2e``       the FP32 form through the C-ABI with the reference host's own
                 FP64 arrays: every step uploads U, V from pinned host memory
                 (mhd_upload_state), steps, and downloads U, V (mhd_download).
 * ``roofline``  the kernel with the largest share of device time, timed live
-                with CUDA events around every launch on the context's stream.
+                with CUDA events around every launch on the context's stream;
+                ``kernel_roofline`` the same for every kernel.
+* ``host_link`` the plain pinned copy rate of this machine's host link.
 * ``cpu_baseline`` the oracle (C restatement of the reference algorithm) on
-                the host cores, on a bounded sample grid of the same physics.
+                the host cores, on the full grid, a bounded number of steps.
 
 ``--impl reference`` times that CPU implementation alone (the reference's
-own C cannot travel to the GPU machine; the restatement is bit-identical to it).
+own C cannot travel to the GPU box; the restatement is bit-identical to it);
+it loads nothing of the product.
 The state is larger than L2 (129 MB), so timed steps run without a flush.
 """
 import argparse
@@ -171,34 +175,40 @@ def time_run(M, disc, steps, warmup, clocks=False):
     return ms, wall, launches, ck
 
 
-def cpu_baseline(M, workload, steps=None, min_seconds=10.0, dims=(128, 128, 64)):
-    """The oracle on all host cores on a bounded sample grid of the workload."""
+def cpu_baseline(workload, dims, steps=2, warmup=1):
+    """The CPU baseline: the oracle (the reference algorithm restated in C,
+    bit-identical to the reference C; oracle/) on all host cores, on the FULL
+    grid of the workload, for a bounded number of steps -- the loop of the
+    reference's main.c:316-393 (Setdt, the dt guard, SpiralGravity when
+    gravity is on, the RK stages).  Grid, knobs and the seeded initial state
+    come from oracle/pyoracle.py, so no product library is loaded."""
     import pyoracle
     threads = os.cpu_count() or 1
-    grid, params, U, V = make_state(M, workload, dims)
-    o = pyoracle.Oracle(grid.spec.as_dict(), M.oracle_params(params), threads=threads)
-    if params.gravity:
-        o.initial_gravity()
-    o.load(U, V)
-    t = 0.0
-    rc, t, *_ = o.step(t)   # warm
-    n = 0
+    (nr, nphi, nz), prm, ic = pyoracle.workload(workload, *dims)
     w0 = time.perf_counter()
-    while True:
+    o = pyoracle.Oracle(pyoracle.gridspec_disc(nr, nphi, nz), prm, threads=threads)
+    if prm["gravity"]:
+        o.initial_gravity()
+    o.ic_disc(**ic)
+    t = 0.0
+    for _ in range(warmup):
         rc, t, *_ = o.step(t)
-        n += 1
-        el = time.perf_counter() - w0
-        if steps is not None and n >= steps:
-            break
-        if steps is None and (el >= min_seconds or n >= 200):
-            break
+        if rc != 0:
+            raise RuntimeError("dt guard fired in the CPU warm-up")
+    setup = time.perf_counter() - w0
+    w0 = time.perf_counter()
+    for _ in range(steps):
+        rc, t, *_ = o.step(t)
+        if rc != 0:
+            raise RuntimeError("dt guard fired in the CPU run")
+    el = time.perf_counter() - w0
     o.close()
-    zones = dims[0] * dims[1] * dims[2]
-    return {"value": zones * n / el, "unit": "zone-updates/s", "cores": threads, "kind": "port",
-            "sample": "%d RK3 steps of the same physics on a %dx%dx%d grid (%d zones), oracle C "
-                      "restatement (bit-identical to the reference C) with OpenMP" %
-                      (n, dims[0], dims[1], dims[2], zones),
-            "seconds": el}
+    zones = nr * nphi * nz
+    return {"value": zones * steps / el, "unit": "zone-updates/s", "cores": threads, "kind": "port",
+            "sample": "%d timed RK3 steps (after %d untimed) of the full %dx%dx%d grid (%d zones), the oracle "
+                      "C restatement of the reference algorithm (bit-identical to the reference C) with "
+                      "OpenMP on %d threads" % (steps, warmup, nr, nphi, nz, zones, threads),
+            "seconds": el, "seconds_per_step": el / steps, "setup_seconds": setup}
 
 
 def precision_report(args):
@@ -456,6 +466,123 @@ def max_over_ranks(dist, x):
     return float(t.item())
 
 
+def select_device(M, local, world):
+    """One process per GPU: bind this rank's device -- its local rank among
+    the visible devices -- before any context exists.  Returns the ordinal
+    (None on one process, which keeps the current device)."""
+    if world <= 1:
+        return None
+    M.use_device(local)
+    return M.current_device()
+
+
+def kernel_bytes(dims, s):
+    """Algorithmic bytes per launch of each kernel: its unique inputs and
+    outputs, s bytes per value (4 in the precision form, 8 in the plain form).
+    A flux kernel reads each cell's 9 primitives once and writes 9 fluxes per
+    face (18 values per face); the update reads V, the three fluxes (27 values
+    with their lower neighbours), U^n, U^(k) in two of the three RK3 stages and
+    the density floor, and writes U and V (70 values per cell averaged over
+    the stages); the CFL reduction reads 8 primitives of the cells of its
+    range (i < ixmax-11)."""
+    nx, ny, nz = dims
+    zones = nx * ny * nz
+    return {"flux_r": (nx + 1) * ny * nz * 18 * s,
+            "flux_phi": nx * (ny + 1) * nz * 18 * s,
+            "flux_z": nx * ny * (nz - 1) * 18 * s,      # interior z faces (the boundary faces run beside them)
+            "update": zones * 70 * s,
+            "setdt": (nx - 10) * ny * nz * 8 * s,
+            "ghost": 0, "trig": 0, "convert": 0,
+            "stage": zones * (9 + 9 + 1 + 9 + 9 + 6) * s,
+            "zupdate": zones * (70 - 9) * s}
+
+
+def kernel_rooflines(kern, nbytes, peak):
+    """Per kernel: algorithmic bytes per launch / mean CUDA-event launch time,
+    against the HBM peak."""
+    out = {}
+    for k, (ms, n) in kern.items():
+        if not n or not nbytes.get(k):
+            continue
+        gbs = nbytes[k] / (ms / n / 1e3) / 1e9
+        out[k] = {"launch_ms": ms / n, "bytes_per_launch": nbytes[k], "gbs": gbs, "frac_hbm": gbs / peak,
+                  "launches": n}
+    return out
+
+
+def e2e_steps(M, disc, U, V, steps, warmup, dist=None):
+    """The metric end to end through the C-ABI: each step uploads U, V from
+    pinned FP64 host arrays (mhd_upload_state), steps (mhd_step) and downloads
+    U, V (mhd_download); each step timed on the context's stream on its own."""
+    Uh = np.ascontiguousarray(U.copy())
+    Vh = np.ascontiguousarray(V.copy())
+    M.pin(Uh)
+    M.pin(Vh)
+    t = 0.0
+    for _ in range(warmup):
+        disc.upload_state(Uh, Vh)
+        rc, t, *_ = disc.step(t)
+        disc.download_into(Uh, Vh)
+    step_ms = []
+    if dist:
+        dist.barrier()
+    for _ in range(steps):
+        disc.timer_start()
+        disc.upload_state(Uh, Vh)
+        rc, t, *_ = disc.step(t)
+        if rc != 0:
+            raise RuntimeError("dt guard fired")
+        disc.download_into(Uh, Vh)
+        step_ms.append(disc.timer_stop())
+    M.pin(Uh, False)
+    M.pin(Vh, False)
+    return step_ms
+
+
+def host_link(M, disc, U, V, reps=2):
+    """Plain pinned host<->device copy rate on this machine: the plain form's
+    mhd_upload_state / mhd_download move U and V with one cudaMemcpyAsync each
+    (no conversion), timed on the context's stream."""
+    Uh = np.ascontiguousarray(U.copy())
+    Vh = np.ascontiguousarray(V.copy())
+    M.pin(Uh)
+    M.pin(Vh)
+    nb = Uh.nbytes + Vh.nbytes
+    up, down = [], []
+    for _ in range(reps + 1):
+        disc.timer_start()
+        disc.upload_state(Uh, Vh)
+        up.append(disc.timer_stop())
+        disc.timer_start()
+        disc.download_into(Uh, Vh)
+        down.append(disc.timer_stop())
+    M.pin(Uh, False)
+    M.pin(Vh, False)
+    return {"h2d_gbs": nb / (min(up[1:]) / 1e3) / 1e9, "d2h_gbs": nb / (min(down[1:]) / 1e3) / 1e9,
+            "bytes": nb, "what": "pinned FP64 U, V: one cudaMemcpyAsync per array (plain form's "
+                                 "mhd_upload_state / mhd_download), best of %d" % reps}
+
+
+def reference_arm(args, dims, cfg):
+    """--impl reference: the reference's algorithm on the CPU (the oracle),
+    full grid, a bounded number of steps; loads no product library."""
+    steps = max(1, min(args.steps, 3))
+    warmup = min(max(args.warmup, 0), 1)
+    cb = cpu_baseline(args.workload, dims, steps=steps, warmup=warmup)
+    out = {"metric": METRIC, "value": cb["value"], "unit": "zone-updates/s", "n_gpus": args.gpus,
+           "steps": steps, "warmup": warmup, "ms_per_step": cb["seconds_per_step"] * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded disc initial state; no public dataset exists)", "impl": "reference",
+           "config": cfg,
+           "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+           "e2e": {"value": cb["value"], "unit": "zone-updates/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0},
+           "note": "each step is a full RK3 step of the stated grid; the arm times min(steps, 3) of them "
+                   "after min(warmup, 1) untimed ones so the run stays within a few minutes"}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -491,30 +618,17 @@ def main():
                        % (args.workload, dims[0], dims[1], dims[2]),
            "zones": zones, "l2": "state (>=2.5 GB) larger than L2; no flush needed"}
     timed_path = ("value: mhd_run, one CUDA graph per RK3 step (CFL reduction and dt on the device); "
-                  "kernel shares/roofline: a separate mhd_step pass with events around each launch; "
+                  "kernel shares/rooflines: a separate mhd_step pass with events around each launch; "
                   "e2e: mhd_upload_state + mhd_step + mhd_download per step")
 
     if args.impl == "reference":
         if rank != 0:
             return 0
-        M = load_product()   # host helpers only (grid + initial state)
-        cb = cpu_baseline(M, args.workload, steps=max(args.steps, 1) + max(args.warmup, 0))
-        out = {"metric": METRIC, "value": cb["value"], "unit": "zone-updates/s", "n_gpus": args.gpus,
-               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-               "config": cfg,
-               "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-               "e2e": {"value": cb["value"], "unit": "zone-updates/s", "h2d_bytes_per_step": 0,
-                       "d2h_bytes_per_step": 0}}
-        print(json.dumps(out))
-        return 0
+        return reference_arm(args, dims, cfg)
 
     dist = dist_init(world)
-    import ctypes
     M = load_product()
-    if world > 1:
-        # one independent replica per GPU (the batched discs do not exchange data)
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    device = select_device(M, local, world)
     grid, params, U, V = make_state(M, args.workload, dims)
     hbm_peak, peak_kind = load_peaks()
 
@@ -525,84 +639,45 @@ def main():
     if dist:
         dist.barrier()
     ms, wall, launches, clocks = time_run(M, d32, args.steps, args.warmup, clocks=(rank == 0))
-    # per-kernel CUDA-event times (for the shares and the roofline) from a
+    # per-kernel CUDA-event times (for the shares and the rooflines) from a
     # separate pass of the same steps through mhd_step, events around each launch
+    nprof = max(3, min(args.steps, 5))
     d32.upload(U, V)
-    _, _, _, kern, _ = time_steps(M, d32, max(3, min(args.steps, 5)), 1, prof=True)
+    _, _, _, kern, _ = time_steps(M, d32, nprof, 1, prof=True)
     ms = max_over_ranks(dist, ms)
     value = zones * args.steps * world / (ms / 1e3)
 
-    # dominant kernel and its roofline (algorithmic bytes, FP32 = 4 B per value)
+    nb32 = kernel_bytes(dims, 4)
+    per_kernel = kernel_rooflines(kern, nb32, hbm_peak)
     tot = sum(v[0] for v in kern.values())
     dom = max(kern, key=lambda k: kern[k][0])
-    dms, dn = kern[dom]
-    s = 4
-    nx, ny, nz_ = dims
-    per_launch = {
-        "flux_r": (nx + 1) * ny * nz_ * 18 * s,      # read V (9), write F (9) per face
-        "flux_phi": nx * (ny + 1) * nz_ * 18 * s,
-        "flux_z": nx * ny * (nz_ + 1) * 18 * s,
-        "update": zones * 64 * s,                    # V, F, G, H (27), U^n, U^k, rhofloor, U, V out
-        "ghost": 0, "setdt": zones * 8 * s, "trig": 0, "convert": 0,
-        # fused stage: V, U^n, rhofloor, U and V out every stage, U^(k) in two of
-        # the three RK3 stages (fluxes stay on chip)
-        "stage": zones * (9 + 9 + 1 + 9 + 9 + 6) * s,
-        # z fluxes + update: the update's bytes less the H round trip
-        "zupdate": zones * (64 - 9) * s,
-    }
-    achieved = per_launch.get(dom, 0) / (dms / dn / 1e3) / 1e9 if dn else None
-    # DRAM bytes (read + write) per zone per launch from the ncu capture of the
-    # first stage of a 256x256x128 step (the split-stage summary under
-    # profiles/), scaled here by the zones of this workload; the update figure
-    # is a first-stage launch (the other two stages also read U^(k))
+    # DRAM bytes (read + write) per zone per launch from the ncu captures at
+    # 256x256x128 (profiles/), scaled here by the zones of this workload
     measured_traffic = {"update": (1.613262e9 + 0.632994e9) / 8388608,
                         "flux_r": (0.384357e9 + 0.262446e9) / 8388608,
                         "flux_phi": (0.382199e9 + 0.262957e9) / 8388608}
     traffic = measured_traffic[dom] * zones if dom in measured_traffic else None
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
+    pk = per_kernel.get(dom, {})
+    roof = {"bound": "hbm", "kernel": dom, "achieved": pk.get("gbs"), "peak": hbm_peak, "unit": "GB/s",
+            "frac": pk.get("frac_hbm"), "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 256x256x128, "
                               "scaled by zones" if traffic else None,
             "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-            "algorithmic_bytes_per_launch": per_launch.get(dom, 0), "avg_launch_ms": dms / dn if dn else None,
-            "note": "stencil with no contraction: the FP32/FP64 pipes, not HBM, bound these kernels; "
-                    "see profiles/ for pipe utilisation"}
+            "algorithmic_bytes_per_launch": pk.get("bytes_per_launch"), "avg_launch_ms": pk.get("launch_ms")}
     shares = {k: round(v[0] / tot, 4) for k, v in kern.items() if v[1]}
-    nprof = max(3, min(args.steps, 5))
-    alg_step = sum(per_launch.get(k, 0) * kern[k][1] for k in kern) / nprof   # algorithmic bytes per step
+    step_ms = ms / args.steps
+    split_bytes = sum(nb32.get(k, 0) * kern[k][1] for k in kern) / nprof   # bytes the split kernels move per step
 
     # ---- e2e through the C-ABI with host FP64 buffers ----
     e2e = None
+    nb = 2 * 9 * grid.ixmax * grid.jymax * grid.kzmax * 8
     if not args.no_e2e:
-        Uh = np.ascontiguousarray(U.copy())
-        Vh = np.ascontiguousarray(V.copy())
-        M.pin(Uh)
-        M.pin(Vh)
-        t = 0.0
-        for _ in range(args.warmup):                     # untimed, like the resident form
-            d32.upload_state(Uh, Vh)
-            rc, t, dt, ch, cnt = d32.step(t)
-            d32.download_into(Uh, Vh)
-        # each step timed on its own (the download returns with the result on
-        # the host, so the steps are serial either way); the sum is the region
-        step_ms = []
-        if dist:
-            dist.barrier()
-        for _ in range(args.steps):
-            d32.timer_start()
-            d32.upload_state(Uh, Vh)
-            rc, t, dt, ch, cnt = d32.step(t)
-            d32.download_into(Uh, Vh)
-            step_ms.append(d32.timer_stop())
-        ems = max_over_ranks(dist, sum(step_ms))
-        M.pin(Uh, False)
-        M.pin(Vh, False)
-        nb = 2 * 9 * grid.ixmax * grid.jymax * grid.kzmax * 8
+        sms = e2e_steps(M, d32, U, V, args.steps, args.warmup, dist)
+        ems = max_over_ranks(dist, sum(sms))
         e2e = {"value": zones * args.steps * world / (ems / 1e3), "unit": "zone-updates/s",
                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "ms_per_step": ems / args.steps,
-               "step_ms_min": min(step_ms), "step_ms_max": max(step_ms),
+               "step_ms_min": min(sms), "step_ms_max": max(sms),
                "what": "mhd_upload_state(U,V) + mhd_step + mhd_download(U,V), FP64 pinned host arrays"}
-        del Uh, Vh
     d32.close()
 
     # ---- plain FP64 form ----
@@ -614,27 +689,47 @@ def main():
         dist.barrier()
     ms64, wall64, l64, kern64, _ = time_steps(M, d64, f64_steps, 1, prof=True)
     ms64 = max_over_ranks(dist, ms64)
-    d64.close()
     v64 = zones * f64_steps * world / (ms64 / 1e3)
+    fp64 = {"value": v64, "unit": "zone-updates/s", "steps": f64_steps, "ms_per_step": ms64 / f64_steps,
+            "speedup_fp32_over_fp64": value / v64,
+            "kernels": kernel_rooflines(kern64, kernel_bytes(dims, 8), hbm_peak)}
+    link = None
+    if not args.no_e2e:
+        d64.upload(U, V)
+        n64e = max(2, min(args.steps, 3))
+        sms = e2e_steps(M, d64, U, V, n64e, 1, dist)
+        ems = max_over_ranks(dist, sum(sms))
+        fp64["e2e"] = {"value": zones * n64e * world / (ems / 1e3), "unit": "zone-updates/s",
+                       "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "steps": n64e,
+                       "ms_per_step": ems / n64e,
+                       "what": "mhd_upload_state(U,V) + mhd_step + mhd_download(U,V), plain FP64 form"}
+        link = host_link(M, d64, U, V)
+    d64.close()
 
     cb = None
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(M, args.workload)
+        cb = cpu_baseline(args.workload, dims, steps=2, warmup=1)
         cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "zone-updates/s", "n_gpus": world,
-               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic (seeded disc initial state; no public dataset exists)",
                "config": cfg, "timed_path": timed_path, "e2e": e2e, "roofline": roof, "cpu_baseline": cb,
                "clocks": clocks,
                "gpu_launches": launches,
                "kernel_share": shares,
-               "fp64": {"value": v64, "unit": "zone-updates/s", "steps": f64_steps,
-                        "ms_per_step": ms64 / f64_steps, "speedup_fp32_over_fp64": value / v64,
-                        "kernel_ms": {k: round(v[0] / max(v[1], 1), 3) for k, v in kern64.items() if v[1]}},
-               "hbm_gbs_algorithmic": alg_step / (ms / args.steps / 1e3) / 1e9}
+               "kernel_roofline": per_kernel,
+               "fp64": fp64,
+               "host_link": link,
+               "step_traffic": {
+                   "split_kernels_gbs": split_bytes / (step_ms / 1e3) / 1e9,
+                   "split_kernels_bytes_per_zone": split_bytes / zones,
+                   "fused_minimum_bytes_per_zone": 300,
+                   "fused_minimum_gbs": 300 * zones / (step_ms / 1e3) / 1e9,
+                   "fused_minimum_frac_hbm": 300 * zones / (step_ms / 1e3) / 1e9 / hbm_peak},
+               "device": device}
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

@@ -14,7 +14,7 @@
  * MHD_ERR_DT instead.  A reference host keeps its globals, array layout
  * ([m][i][j][k], k fastest, FP64, one ghost cell per side) and file formats;
  * it hands its arrays to mhd_create()/mhd_upload() once and calls the step
- * functions in place of its own.  INTEGRATION.md shows the calls.
+ * functions in place of its own.
  *
  * Conventions: every function returns 0 (MHD_OK) or a negative MHD_ERR_*
  * code; nothing prints or exits.  A context is used by one host thread at a
@@ -186,6 +186,14 @@ int mhd_gnu_output_cylinder(const char *root, int nout, int nstep, double t, con
 int mhd_gdl_output_cylinder(const char *root, int nout, const mhd_grid *g, const double *V);
 
 /* ---- device context: the step ------------------------------------------- */
+/* A context binds the calling thread's current CUDA device at mhd_create().
+ * mhd_use_device() makes device `ordinal` (0-based among the visible devices)
+ * current for the calling thread -- one process per GPU calls it with its
+ * local rank before its first mhd_create(); MHD_ERR_ARG for an ordinal
+ * outside [0, device count), MHD_ERR_NODEV without a CUDA device.
+ * mhd_current_device() returns the calling thread's current ordinal. */
+int mhd_use_device(int ordinal);
+int mhd_current_device(int *ordinal);
 int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out);
 void mhd_destroy(mhd_ctx *ctx);
 /* State upload, host layout [9][ixmax][jymax][kzmax] FP64 (commonfield.h:114,
@@ -252,7 +260,11 @@ int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg);
  * cells in shared memory with tensor copies, where the layout allows it
  * (cells per variable a multiple of 4).  MHD_ERR_ARG for tma = 1 where it is
  * not available (plain form, other layouts).  A tile whose copies do not
- * land within a bounded wait makes the step return MHD_ERR_TIMEOUT. */
+ * land within a bounded wait makes the step return MHD_ERR_TIMEOUT.  That
+ * give-up path waits a second bounded time for the copies still in flight;
+ * should that wait also run out, the block exits with bulk copies possibly
+ * still writing its shared memory, which is unsafe -- the option stays off
+ * by default, and no test drives either wait to its limit. */
 int mhd_set_update_path(mhd_ctx *ctx, int tma);
 /* 1 if the split stage's update is TMA-staged, 0 if not. */
 int mhd_update_path(const mhd_ctx *ctx);
@@ -323,8 +335,13 @@ int mhd_batch_debug_stall(mhd_batch *b, int disc, int spin_limit);
  * [ix+2][kz+2]; dt, ch, ijk are host outputs as for mhd_setdt().  Grids whose
  * CFL range (ix-10)*jy*kz exceeds MHD_NOALLOC_MAX_BLOCKS*256*64 cells
  * (134,217,728) are rejected with MHD_ERR_ARG before any launch.  The first
- * call on a device looks up the array's device address (make it before any
- * stream capture).  Calls share the array: calls that overlap on the GPU
+ * call on a device looks up the array's device address and caches it for the
+ * process; with CUDA's default lazy module loading that first call may also
+ * be what loads this code onto the device and maps the array, so make it at
+ * start-up, before the no-allocation window opens and before any stream
+ * capture.  The cached address does not survive a device reset
+ * (cudaDeviceReset or a torn-down primary context): calling again after one
+ * is not supported.  Calls share the array: calls that overlap on the GPU
  * race and must be serialised by the caller. */
 #define MHD_NOALLOC_MAX_BLOCKS 8192
 int mhd_setdt_noalloc(const double *V, const double *minlength, int ix, int jy, int kz, double cfl,

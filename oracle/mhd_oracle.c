@@ -363,6 +363,75 @@ void orc_load(orc_ctx *o, const double *U, const double *V, const double *Uinit,
     memcpy(o->rhofloor, rhofloor, o->nc * sizeof(double));
 }
 
+/* The benchmark's seeded disc, generated in place so a full-size CPU run needs
+ * no second copy of the state: rho = exp(-z^2/(2*0.1^2)) + 1e-3, p = 0.01 rho,
+ * v_phi = 1, B_phi = sqrt(2p/beta), with uniform [-1,1) perturbations of
+ * relative size amp on rho and of size amp on v (four splitmix64 draws per
+ * cell, cells in [i][j][k] order, ghosts included).  Then VtoU (vtou.h:20-62)
+ * and SaveInitial's copies and density floor (saveinitial.h:30-41). */
+static unsigned long long orc_splitmix64(unsigned long long *s)
+{
+    unsigned long long z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+static double orc_unit_pm(unsigned long long *s)
+{
+    return 2.0 * ((double)(orc_splitmix64(s) >> 11) * 0x1.0p-53) - 1.0;
+}
+
+void orc_ic_disc(orc_ctx *o, double beta, double amp, unsigned long long seed)
+{
+    const size_t nc = o->nc;
+    unsigned long long st = seed;
+    size_t q = 0;
+    for (int i = 0; i < o->ixmax; i++)
+        for (int j = 0; j < o->jymax; j++)
+            for (int k = 0; k < o->kzmax; k++, q++) {
+                double zk = o->z[k];
+                double rho = exp(-zk * zk / (2.0 * 0.1 * 0.1)) + 1.0e-3;
+                double ur = orc_unit_pm(&st), uvr = orc_unit_pm(&st), uvp = orc_unit_pm(&st), uvz = orc_unit_pm(&st);
+                rho = rho * (1.0 + amp * ur);
+                double pr = 0.01 * rho;
+                double *v = o->V;
+                v[q] = rho;
+                v[nc + q] = amp * uvr;
+                v[2 * nc + q] = 1.0 + amp * uvp;
+                v[3 * nc + q] = amp * uvz;
+                v[4 * nc + q] = 0.0;
+                v[5 * nc + q] = sqrt(2.0 * pr / beta);
+                v[6 * nc + q] = 0.0;
+                v[7 * nc + q] = pr;
+                v[8 * nc + q] = 0.0;
+            }
+#pragma omp parallel for
+    for (int i = 0; i < o->ixmax; i++) {
+        const double xi = o->x[i];
+        for (size_t c = (size_t)i * o->jymax * o->kzmax; c < (size_t)(i + 1) * o->jymax * o->kzmax; c++) {
+            const double *v = o->V;
+            double *u = o->U;
+            double v2 = v[nc + c] * v[nc + c] + v[2 * nc + c] * v[2 * nc + c] + v[3 * nc + c] * v[3 * nc + c];
+            double b2 = v[4 * nc + c] * v[4 * nc + c] + v[5 * nc + c] * v[5 * nc + c] + v[6 * nc + c] * v[6 * nc + c];
+            u[c] = v[c];
+            u[nc + c] = v[c] * v[nc + c];
+            u[2 * nc + c] = xi * v[c] * v[2 * nc + c];
+            u[3 * nc + c] = v[c] * v[3 * nc + c];
+            u[4 * nc + c] = v[4 * nc + c];
+            u[5 * nc + c] = v[5 * nc + c];
+            u[6 * nc + c] = v[6 * nc + c];
+            u[7 * nc + c] = 0.5 * (v[c] * v2 + b2) + ONEOGM1 * v[7 * nc + c];
+            u[8 * nc + c] = v[8 * nc + c];
+            for (int m = 0; m < 9; m++) {
+                o->Uinit[m * nc + c] = u[m * nc + c];
+                o->Vinit[m * nc + c] = v[m * nc + c];
+            }
+            o->rhofloor[c] = u[c] * o->p.rhocr;
+        }
+    }
+}
+
 void orc_store(const orc_ctx *o, double *U, double *V, double *U1)
 {
     size_t n9 = 9 * o->nc * sizeof(double);

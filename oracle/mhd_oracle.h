@@ -68,6 +68,8 @@ void orc_get_gravity(const orc_ctx *o, double *axi, double *gr);
 void orc_load(orc_ctx *o, const double *U, const double *V, const double *Uinit,
               const double *Vinit, const double *rhofloor);
 void orc_store(const orc_ctx *o, double *U, double *V, double *U1);
+/* the benchmark's seeded disc (V, U, Uinit, Vinit, rhofloor) set in place */
+void orc_ic_disc(orc_ctx *o, double beta, double amp, unsigned long long seed);
 
 void orc_setdt(orc_ctx *o, double *dt, double *ch, int *ijk);   /* setdt.h:24 */
 void orc_spiral_gravity(orc_ctx *o, double t);                 /* spiralgravity.h:20 */

@@ -36,6 +36,64 @@ class _Params(C.Structure):
     _fields_ = [(f, C.c_double) for f in PARAM_FIELDS] + [(f, C.c_int) for f in FLAG_FIELDS]
 
 
+# ---------------------------------------------------------------------------
+# the benchmark's disc workloads, defined here too so that the CPU legs (the
+# reference arm and the CPU baseline) run without loading the product library
+# ---------------------------------------------------------------------------
+
+def default_params(**over):
+    """The reference's knobs (input.h:58-102, constant.h:62-79) as a dict."""
+    year, t0, kpc = 3.1536e+7, 4.7058e+15, 3.08568e+21
+    omega0, oneokpc = 1.0 / t0, 1.0 / kpc
+    p = dict(cfl=0.4, dtmin=1.0e-9, rhocr=1.0e-4, prcr=0.015, betacr=0.1, epssp0=0.05,
+             tausp=200.0 * 1.0e+6 * year / t0, scalez=0.03, scaler=0.7, scalephase=0.1, armnum=2.0,
+             omegasp=10.0e+5 / omega0 * oneokpc, omegapattern=10.0e+5 / omega0 * oneokpc,
+             pitch=15.0 * np.pi / 180.0, limiter=0, solver=0, scheme=2, cooling=1, gravity=1, source=0)
+    named = {"limiter": {"minmod": 0, "mc": 1, "vanleer": 2, "superbee": 3},
+             "solver": {"hlld": 0, "hll": 1}}
+    for k, v in over.items():
+        if k in named and isinstance(v, str):
+            v = named[k][v]
+        if k == "precision":
+            continue
+        p[k] = float(v) if k == "armnum" else v
+    return p
+
+
+def gridspec_disc(nr, nphi, nz):
+    """The uniform disc grid r in [0.1,1.5], phi in [0,2pi), z in [-0.5,0.5]
+    in the reference's input.h terms (x0 = first cell centre, stretching
+    pushed beyond the domain)."""
+    dx0, dz0 = 1.4 / nr, 1.0 / nz
+    return dict(ix=nr, jy=nphi, kz=nz, x0=0.1 + 0.5 * dx0, dx0=dx0, lx=1.0e30, y0=0.0, ly=2.0 * np.pi,
+                z0=-0.5 + 0.5 * dz0, dz0=dz0, lz=1.0e30, stretchratio=1.05, dxmax=50.0 * dx0,
+                dzmax=50.0 * dz0, rin=0.1)
+
+
+def workload(name, nr=None, nphi=None, nz=None, **over):
+    """dims, params dict and initial-condition arguments of a named disc
+    workload (the same definitions as the product binding's workload())."""
+    base = dict(limiter="minmod", solver="hlld", scheme=3, cooling=0, gravity=0, prcr=1.0e-3,
+                rhocr=1.0e-4, betacr=0.1, cfl=0.4, omegasp=0.0)
+    if name == "disc1":
+        dims, beta = (64, 64, 32), 10.0
+    elif name == "disc2":
+        dims, beta = (256, 256, 128), 1.0
+        base.update(limiter="mc", gravity=1, cooling=1, epssp0=0.03, omegapattern=0.5,
+                    pitch=15.0 * np.pi / 180.0, armnum=2)
+    elif name == "disc3":
+        dims, beta = (256, 256, 128), 10.0
+    elif name == "disc5":
+        dims, beta = (512, 512, 256), 1.0
+        base.update(cooling=1)
+    else:
+        raise ValueError(name)
+    dims = (nr or dims[0], nphi or dims[1], nz or dims[2])
+    beta = over.pop("beta", beta)
+    base.update(over)
+    return dims, default_params(**base), dict(beta=beta, amp=0.01, seed=0)
+
+
 def build_oracle(force=False):
     """Compile oracle/mhd_oracle.c (here or on the GPU machine) and return the path."""
     src = os.path.join(HERE, "mhd_oracle.c")
@@ -171,6 +229,7 @@ class Oracle(_Common):
             lib.orc_utov_check.argtypes = [vp, _DP, _DP, _IP]
             lib.orc_cooling.restype = C.c_int
             lib.orc_cooling.argtypes = [C.c_double, C.c_double]
+            lib.orc_ic_disc.argtypes = [vp, C.c_double, C.c_double, C.c_ulonglong]
             cls._lib = lib
         return cls._lib
 
@@ -206,6 +265,12 @@ class Oracle(_Common):
 
     def initial_gravity(self):
         self.lib().orc_initial_gravity(self.h)
+
+    def ic_disc(self, beta, amp=0.01, seed=0):
+        """The seeded disc state set in place (orc_ic_disc): V, U, the
+        initial copies and the density floor."""
+        self.lib().orc_set_threads(self.threads)
+        self.lib().orc_ic_disc(self.h, float(beta), float(amp), int(seed))
 
     def set_gravity_axi(self, axi):
         self.lib().orc_set_gravity_axi(self.h, _f64(axi))

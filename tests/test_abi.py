@@ -67,3 +67,15 @@ def test_grid_storage_layout(M):
     assert g.irin == int(0.1 / (1.4 / 24))
     z = g.arr("z", g.kzmax)
     assert np.isclose(z[1], -0.5 + 0.5 / 20) and np.isclose(z[-2], 0.5 - 0.5 / 20)
+
+
+def test_device_selection_errors_are_codes(M):
+    L = M.lib()
+    d = C.c_int(-1)
+    rc0 = L.mhd_use_device(0)
+    if rc0 == -7:          # no CUDA device here: every call says so, none crashes
+        assert L.mhd_use_device(-1) == -7 and L.mhd_current_device(C.byref(d)) == -7
+    else:
+        assert rc0 == 0 and L.mhd_use_device(-1) == -1 and L.mhd_use_device(1 << 20) == -1
+        assert L.mhd_current_device(C.byref(d)) == 0 and d.value == 0
+    assert L.mhd_current_device(None) == -1
