@@ -190,6 +190,10 @@ static void free_all(mhd_ctx *ctx)
         if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    for (int q = 0; q < MHD_MAX_SLABS; q++)
+        if (ctx->ev_slab[q]) cudaEventDestroy(ctx->ev_slab[q]);
+    if (ctx->ev_upd) cudaEventDestroy(ctx->ev_upd);
+    if (ctx->st_upd) { cudaStreamSynchronize(ctx->st_upd); cudaStreamDestroy(ctx->st_upd); }
     if (ctx->st_aux) { cudaStreamSynchronize(ctx->st_aux); cudaStreamDestroy(ctx->st_aux); }
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx->maps;
@@ -261,6 +265,10 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     ctx->stage_seg = 32;
     memset((void *)&ctx->G, 0, sizeof ctx->G);
     cudaGetDevice(&ctx->device);
+    if (cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || ctx->nsm < 1) {
+        cudaGetLastError();
+        ctx->nsm = 152;
+    }
     ctx->p = *p;
     ctx->ix = g->ix; ctx->jy = g->jy; ctx->kz = g->kz;
     ctx->ixmax = g->ix + 2; ctx->jymax = g->jy + 2; ctx->kzmax = g->kz + 2;
@@ -675,8 +683,46 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.trigf = ctx->d_trigf; a.kind = kind; a.last = last; a.counters = counters;
     a.Vinit = Vinit;
     a.zghost = ctx->fused == 0;   /* the split update fills the interior columns' k-plane ghosts */
+    /* path 2: each update block prefetches the block one wave ahead into L2
+     * (8 resident blocks of 128 threads per SM in the precision form) */
+    a.prefetch = ctx->upd_tma == 2 ? 8 * ctx->nsm : 0;
     if (ctx->fused == 1) {
         LAUNCH(PK_STAGE, launch_stage(ctx->G, a, ctx->stage_tj, ctx->stage_seg, ctx->st));
+    } else if (ctx->fused == 3) {
+        /* the split kernels pipelined over ns slabs of i planes: the fluxes of
+         * slab s on the context's stream, then its update on the update
+         * stream, so the update of slab s (HBM-bound) runs beside the fluxes
+         * of slab s+1 (issue-bound).  Slab s [a, b) needs the r faces a-1 ..
+         * b-1; slab 0 computes faces 0 .. b-1 and slab s > 0 faces a .. b-1
+         * (face a-1 is the slab before's), so every face is computed once and
+         * the update of slab s waits only for the fluxes through slab s. */
+        const int ni = ctx->ixmax - 2;
+        const int ns = ctx->stage_seg < ni ? ctx->stage_seg : ni;
+        CK(cudaEventRecord(ctx->ev_fork, ctx->st));
+        CK(cudaStreamWaitEvent(ctx->st_upd, ctx->ev_fork, 0));
+        for (int sl = 0; sl < ns; sl++) {
+            const int a0 = 1 + (int)((long long)ni * sl / ns), b0 = 1 + (int)((long long)ni * (sl + 1) / ns);
+            Box br = flux_box(ctx, 0), bp = flux_box(ctx, 1), bz = flux_box(ctx, 2);
+            br.i0 = sl == 0 ? 0 : a0;
+            br.i1 = b0;
+            bp.i0 = bz.i0 = a0;
+            bp.i1 = bz.i1 = b0;
+            LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, br, false, ctx->st));
+            LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, bp, false, ctx->st));
+            CK(launch_zedge(ctx->G, V, Vinit, ctx->d_sc, H, bz, ctx->st));
+            ctx->launches++;
+            LAUNCH(PK_FLUX_Z, launch_flux_zinterior(ctx->G, V, Vinit, ctx->d_sc, H, bz, ctx->st));
+            CK(cudaEventRecord(ctx->ev_slab[sl], ctx->st));
+            CK(cudaStreamWaitEvent(ctx->st_upd, ctx->ev_slab[sl], 0));
+            a.ibeg = a0;
+            a.iend = b0;
+            CK(launch_update(ctx->G, a, ctx->st_upd));
+            ctx->launches++;
+        }
+        a.ibeg = 1;
+        a.iend = 0;
+        CK(cudaEventRecord(ctx->ev_upd, ctx->st_upd));
+        CK(cudaStreamWaitEvent(ctx->st, ctx->ev_upd, 0));
     } else if (ctx->fused == 2) {
         LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
         LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
@@ -693,7 +739,7 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
         CK(cudaEventRecord(ctx->ev_join, ctx->st_aux));
         LAUNCH(PK_FLUX_Z, launch_flux_zinterior(ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), ctx->st));
         CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
-        if (ctx->upd_tma)
+        if (ctx->upd_tma == 1)
             LAUNCH(PK_UPDATE, launch_update_tma(ctx->G, a, *ctx->maps, ctx->vcur, &ctx->d_sc->err, ctx->st));
         else
             LAUNCH(PK_UPDATE, launch_update(ctx->G, a, ctx->st));
@@ -1149,7 +1195,15 @@ extern "C" int mhd_prof_enable(mhd_ctx *ctx, int on)
 
 extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
 {
-    if (!ctx || fused < 0 || fused > 2 || tj != 7 || seg < 1) return MHD_ERR_ARG;
+    if (!ctx || fused < 0 || fused > 3 || seg < 1 || (fused != 3 && tj != 7) || (fused == 3 && seg > MHD_MAX_SLABS))
+        return MHD_ERR_ARG;
+    if (fused == 3 && !ctx->st_upd) {
+        int lo = 0, hi = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        CK(cudaStreamCreateWithPriority(&ctx->st_upd, cudaStreamNonBlocking, hi));
+        for (int q = 0; q < MHD_MAX_SLABS; q++) CK(cudaEventCreateWithFlags(&ctx->ev_slab[q], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->ev_upd, cudaEventDisableTiming));
+    }
     ctx->fused = fused;
     ctx->stage_tj = tj;
     ctx->stage_seg = seg;
@@ -1165,7 +1219,7 @@ extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
 
 extern "C" int mhd_set_update_path(mhd_ctx *ctx, int tma)
 {
-    if (!ctx || tma < 0 || tma > 1 || (tma && !ctx->maps)) return MHD_ERR_ARG;
+    if (!ctx || tma < 0 || tma > 2 || (tma == 1 && !ctx->maps) || (tma == 2 && !ctx->fp32)) return MHD_ERR_ARG;
     ctx->upd_tma = tma;
     if (ctx->graph_ready) {
         CK(cudaStreamSynchronize(ctx->st));
@@ -1173,6 +1227,13 @@ extern "C" int mhd_set_update_path(mhd_ctx *ctx, int tma)
             if (ctx->gexecs[q]) { cudaGraphExecDestroy(ctx->gexecs[q]); ctx->gexecs[q] = NULL; }
         ctx->graph_ready = 0;
     }
+    return MHD_OK;
+}
+
+extern "C" int mhd_set_state_rounding(mhd_ctx *ctx, int on)
+{
+    if (!ctx || ctx->fp32 || on < 0 || on > 1) return MHD_ERR_ARG;
+    ctx->G.round_state = on;
     return MHD_OK;
 }
 

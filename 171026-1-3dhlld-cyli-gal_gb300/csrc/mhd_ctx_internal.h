@@ -14,12 +14,18 @@
 #include "mhd_launch.h"
 
 #define NSTAGE 4   /* staging buffers (and copy streams) of the precision form's host transfers */
+#define MHD_MAX_SLABS 64   /* slabs of the pipelined split stage (stage shape 3) */
 
 struct mhd_ctx {
     int device;
+    int nsm;                     /* multiprocessors of the device */
     cudaStream_t st;
     cudaStream_t st_aux;         /* the z boundary faces beside the interior z faces */
     cudaEvent_t ev_fork, ev_join;
+    /* stage shape 3: the update of each slab of i planes on its own stream
+     * (highest priority) beside the fluxes of the following slabs */
+    cudaStream_t st_upd;
+    cudaEvent_t ev_slab[MHD_MAX_SLABS], ev_upd;
     mhd_params p;
     int ix, jy, kz, ixmax, jymax, kzmax, irin;
     long long nc;
@@ -34,7 +40,9 @@ struct mhd_ctx {
      * separate kernels), tile height tj (j) and run length seg (i) */
     int fused, stage_tj, stage_seg;
     /* tensor maps of the TMA-staged update (precision form, when the layout
-     * allows it; else NULL) and whether the split stage uses it */
+     * allows it; else NULL) and how the split stage's update reads its inputs:
+     * 0 thread loads, 1 TMA-staged tiles, 2 thread loads with an L2 prefetch
+     * of the block one wave ahead */
     mhd::UpdMaps *maps;
     int upd_tma;
     mhd::StepScalars *d_sc, *h_sc;

@@ -286,6 +286,7 @@ __device__ __forceinline__ void zghost_fill(const Geom &G, const StageArgs<T> &a
     for (int m = 0; m < 9; m++) ug[m] = (flip && m == 3) ? -u[m] : u[m];
     if (a.last) absorb<T>(G, a.Uinit, i, j, kg, G.scheme == MHD_SCHEME_RK2, ug);
     const int flags = utov_check<T>(G, i, a.rhofloor[qg], ug, W);
+    round_stored<T>(G, ug, W);
     T *Uo = (a.kind == 0 || a.kind == 1) ? a.U1 : a.Un;
 #pragma unroll
     for (int m = 0; m < 9; m++) { Uo[m * nc + qg] = ug[m]; a.Vout[m * nc + qg] = W[m]; }
@@ -325,12 +326,25 @@ __device__ __forceinline__ int update_core(const Geom &G, const StageArgs<T> &a,
 #pragma unroll
     for (int m = 0; m < 9; m++) {
         T un = in.un(m), u1 = (kind == 0) ? T(0) : in.u1(m);
-        if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
         T v;
-        if (kind == 0) v = un - dt * div[m] + dt * S[m];
-        else if (kind == 1) v = T(0.25) * (T(3.0) * un + u1 - dt * div[m] + dt * S[m]);
-        else if (kind == 2) v = T(MHD_ONEO3) * (un + T(2.0) * (u1 - dt * div[m] + dt * S[m]));
-        else v = T(0.5) * (un + u1 - dt * div[m] + dt * S[m]);
+        if (sizeof(T) == 4) {
+            /* precision form: one rounding per stage (stage_combine) */
+            float eun = 0.0f, eu1 = 0.0f;
+            if (m == 8) {   /* GLMSourceSolver on U and U1, product residuals kept */
+                const float pn = (float)psicoef * (float)un, p1 = (float)psicoef * (float)u1;
+                eun = fmaf((float)psicoef, (float)un, -pn);
+                eu1 = fmaf((float)psicoef, (float)u1, -p1);
+                un = pn;
+                u1 = p1;
+            }
+            v = (T)stage_combine(kind, (float)un, (float)u1, (float)dt, (float)div[m], (float)S[m], eun, eu1);
+        } else {
+            if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
+            if (kind == 0) v = un - dt * div[m] + dt * S[m];
+            else if (kind == 1) v = T(0.25) * (T(3.0) * un + u1 - dt * div[m] + dt * S[m]);
+            else if (kind == 2) v = T(MHD_ONEO3) * (un + T(2.0) * (u1 - dt * div[m] + dt * S[m]));
+            else v = T(0.5) * (un + u1 - dt * div[m] + dt * S[m]);
+        }
         u[m] = v;
     }
     if (is_bc_source(G, i, j, k)) {
@@ -341,6 +355,7 @@ __device__ __forceinline__ int update_core(const Geom &G, const StageArgs<T> &a,
     if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);   /* zboundary.h:87 */
     if (a.last) absorb<T>(G, a.Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
     int flags = utov_check<T>(G, i, in.rho(), u, W);
+    round_stored<T>(G, u, W);
     T *Uo = (kind == 0 || kind == 1) ? a.U1 : a.Un;
 #pragma unroll
     for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; a.Vout[m * nc + q] = W[m]; }
@@ -372,12 +387,53 @@ __device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a,
 }
 
 template <typename T>
+__device__ __forceinline__ void prefetch_run(const T *p, long long n, long long e0, long long e1);
+
+/* The update's streamed inputs of the block a.prefetch blocks ahead (in
+ * launch order, about one wave of resident blocks), prefetched into L2 by
+ * the first warp with bulk prefetches: V, F, G, H, U^n, U^(k) and the
+ * density floor rows of that block's cells (the F and G rows one plane and
+ * one row lower were prefetched for earlier blocks).  Each block then finds
+ * its inputs in L2, so the DRAM reads run a wave ahead without holding
+ * registers or shared memory. */
+template <typename T>
+__device__ __forceinline__ void update_prefetch_ahead(const Geom &G, const StageArgs<T> &a)
+{
+    const int lane = threadIdx.x + blockDim.x * threadIdx.y;
+    if (lane >= 32) return;
+    const long long nb = (long long)gridDim.x * gridDim.y * gridDim.z;
+    const long long b = (long long)blockIdx.x + gridDim.x * ((long long)blockIdx.y + (long long)gridDim.y * blockIdx.z)
+                        + a.prefetch;
+    if (b >= nb) return;
+    const int bx = (int)(b % gridDim.x), by = (int)((b / gridDim.x) % gridDim.y), bz = (int)(b / ((long long)gridDim.x * gridDim.y));
+    const int k0 = 1 + bx * blockDim.x, i = a.ibeg + bz;
+    const int kn = min((int)blockDim.x, G.kzmax - 1 - k0);
+    const long long nc = G.nc, n9 = 9 * nc;
+    for (int t = lane; t < 7 * (int)blockDim.y * 9; t += 32) {
+        const int arr = t / (9 * blockDim.y), rem = t % (9 * blockDim.y), m = rem / blockDim.y;
+        const int j = 1 + by * blockDim.y + rem % blockDim.y;
+        if (j >= G.jymax - 1 || kn <= 0) continue;
+        const long long q = cidx(G, i, j, k0) + m * nc;
+        switch (arr) {
+        case 0: prefetch_run<T>(a.V, n9, q, q + kn); break;
+        case 1: prefetch_run<T>(a.F, n9, q, q + kn); break;
+        case 2: prefetch_run<T>(a.G, n9, q, q + kn); break;
+        case 3: prefetch_run<T>(a.H, n9, q - 1, q + kn); break;
+        case 4: prefetch_run<T>(a.Un, n9, q, q + kn); break;
+        case 5: if (a.kind != 0) prefetch_run<T>(a.U1, n9, q, q + kn); break;
+        default: if (m == 0) prefetch_run<T>(a.rhofloor, nc, q, q + kn); break;
+        }
+    }
+}
+
+template <typename T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1) update_kernel(Geom G, StageArgs<T> a)
 {
     if (a.sc->dtbad) return;
+    if (a.prefetch) update_prefetch_ahead<T>(G, a);
     const int k = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = 1 + blockIdx.z;
+    const int i = a.ibeg + blockIdx.z;
     int flags = 0;
     if (k < G.kzmax - 1 && j < G.jymax - 1) flags = update_cell<T>(G, a, i, j, k);
     add_counters(flags, a.counters);
@@ -395,7 +451,10 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1) update_kernel(Geo
  * several tiles (about 40 KB each) in flight; the update itself is
  * update_core, one thread per cell, ghost cells skipped.  The wait is bounded:
  * a tile whose copies do not land within `spin` polls sets *err, waits as long
- * again for the copies still in flight and leaves the tile untouched.
+ * again for the copies still in flight and leaves the tile untouched.  Should
+ * that second wait run out as well, the block exits while bulk copies may
+ * still be writing its shared memory -- unsafe, which is one reason this path
+ * is an option that stays off, and no test drives either wait to its limit.
  * Measured at 512x512x256: 3.62 ms per launch against 3.38 ms for
  * update_kernel (3.69 ms with all on-chip memory as shared memory): five
  * 38 KB tiles per SM keep more bytes in flight than the thread loads, but
@@ -828,6 +887,7 @@ __device__ __forceinline__ int ghost_cell(const Geom &G, const StageArgs<T> &a, 
     if (G.scheme == MHD_SCHEME_RK2 && k == 1) u[3] = T(0.0);
     if (a.last) absorb<T>(G, a.Uinit, i, j, k, G.scheme == MHD_SCHEME_RK2, u);
     int flags = utov_check<T>(G, i, a.rhofloor[q], u, W);
+    round_stored<T>(G, u, W);
     T *Uo = (a.kind == 0 || a.kind == 1) ? a.U1 : a.Un;
 #pragma unroll
     for (int m = 0; m < 9; m++) { Uo[m * nc + q] = u[m]; a.Vout[m * nc + q] = W[m]; }
@@ -1100,8 +1160,11 @@ cudaError_t launch_states_t(int dir, const Geom &G, const T *V, const T *Vinit, 
 template <typename T>
 cudaError_t launch_update_t(const Geom &G, const StageArgs<T> &a, cudaStream_t st)
 {
+    const int i1 = a.iend > 0 ? a.iend : G.ixmax - 1;
+    if (a.ibeg < 1 || i1 > G.ixmax - 1) return cudaErrorInvalidValue;
+    if (i1 <= a.ibeg) return cudaSuccess;
     dim3 gr, bl;
-    grid3(G.kzmax - 2, G.jymax - 2, G.ixmax - 2, gr, bl);
+    grid3(G.kzmax - 2, G.jymax - 2, i1 - a.ibeg, gr, bl);
     update_kernel<T><<<gr, bl, 0, st>>>(G, a);
     return cudaGetLastError();
 }

@@ -137,6 +137,7 @@ def lib():
         "mhd_set_stage_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
         "mhd_set_update_path": (C.c_int, [vp, C.c_int]),
         "mhd_update_path": (C.c_int, [vp]),
+        "mhd_set_state_rounding": (C.c_int, [vp, C.c_int]),
         "mhd_prof_read": (C.c_int, [vp, DP, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]),
         "mhd_launch_count": (C.c_longlong, [vp]),
         "mhd_timer_start": (C.c_int, [vp]),
@@ -501,6 +502,11 @@ class Disc:
         """1: the split stage's update stages its tiles in shared memory with
         tensor copies; 0: thread-by-thread loads (mhd_set_update_path)."""
         check(lib().mhd_set_update_path(self.h, int(tma)), "mhd_set_update_path")
+
+    def set_state_rounding(self, on=True):
+        """Plain form only: FP64 arithmetic, U and V stored rounded to FP32 after
+        every stage -- the FP32-storage error floor (mhd_set_state_rounding)."""
+        check(lib().mhd_set_state_rounding(self.h, 1 if on else 0), "mhd_set_state_rounding")
 
     def update_path(self):
         return int(lib().mhd_update_path(self.h))

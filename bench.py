@@ -215,11 +215,13 @@ def precision_report(args):
     """FP32 + FP64-repair form against the plain FP64 form (bit-identical to the
     reference C, checked on smaller grids by the tests) after N steps from the
     same state: per conserved variable relative L1 and Linf, and the drift of
-    the totals and max|div B| of both forms.  The same comparison for a plain
-    FP64 run started from the FP32-rounded state (fp64_twin) gives the floor:
-    the part of the difference a rounding-sized perturbation of the start
-    produces by itself.  m_r, m_z (against sum |rho v_phi|) and B_r, B_z, psi
-    (against sum |B|) are also reported relative to the flow's scales."""
+    the totals and max|div B| of both forms.  Two plain-form runs give the
+    floors: fp64_twin starts from the FP32-rounded state (what one rounding of
+    the start produces by itself), fp32_storage_floor also rounds U and V to
+    FP32 after every stage with FP64 arithmetic (what FP32 state storage alone
+    produces -- no form that stores FP32 state does better).  m_r, m_z
+    (against sum |rho v_phi|) and B_r, B_z, psi (against sum |B|) are also
+    reported relative to the flow's scales."""
     M = load_product()
     dims = tuple(int(v) for v in args.size.split("x")) if args.size else (256, 256, 128)
     (nr, nphi, nz), params, ic = M.workload(args.workload, nr=dims[0], nphi=dims[1], nz=dims[2],
@@ -235,9 +237,11 @@ def precision_report(args):
     # a rounding-sized perturbation of the start alone carries in N steps
     U32 = U.astype(np.float32).astype(np.float64)
     V32 = V.astype(np.float32).astype(np.float64)
-    for prec in ("fp64", "fp32", "fp64_twin"):
-        d = M.Disc(grid, with_precision(M, params, "fp64" if prec == "fp64_twin" else prec))
-        if prec == "fp64_twin":
+    for prec in ("fp64", "fp32", "fp64_twin", "fp32_storage_floor"):
+        d = M.Disc(grid, with_precision(M, params, "fp32" if prec == "fp32" else "fp64"))
+        if prec == "fp32_storage_floor":
+            d.set_state_rounding(True)
+        if prec in ("fp64_twin", "fp32_storage_floor"):
             d.upload(U32, V32)
         else:
             d.upload(U, V)
@@ -285,6 +289,7 @@ def precision_report(args):
 
     out["fp32_vs_fp64"] = compare(res["fp32"])
     out["fp64_twin_vs_fp64"] = compare(res["fp64_twin"])
+    out["fp32_storage_floor_vs_fp64"] = compare(res["fp32_storage_floor"])
     print(json.dumps(out))
     return 0
 

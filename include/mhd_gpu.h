@@ -253,20 +253,32 @@ int mhd_prof_read(mhd_ctx *ctx, double ms[MHD_PROF_NKIND], long long launches[MH
  * kernels, then one kernel forms the z fluxes in registers and updates the
  * cells; fused = 1: one kernel forms all fluxes on chip and updates the cells
  * (tile 32 k-cells x tj j-cells, tj = 7, marching over runs of seg cells in
- * r).  All give the same bits in the plain form. */
+ * r); fused = 3: the kernels of fused = 0 pipelined over seg slabs of i
+ * planes (1..64; tj ignored), the update of each slab on a second,
+ * higher-priority stream beside the fluxes of the next slabs.  All give the
+ * same bits in the plain form. */
 int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg);
 /* How the split stage's update reads its inputs (precision form): tma = 0
  * (the default) loads them thread by thread; tma = 1 stages each tile of 128
  * cells in shared memory with tensor copies, where the layout allows it
  * (cells per variable a multiple of 4).  MHD_ERR_ARG for tma = 1 where it is
- * not available (plain form, other layouts).  A tile whose copies do not
- * land within a bounded wait makes the step return MHD_ERR_TIMEOUT.  That
+ * not available (plain form, other layouts); tma = 2 (precision form) keeps
+ * the thread loads and has each block prefetch the streamed inputs of the
+ * block one wave of resident blocks ahead into L2.  With tma = 1, a tile
+ * whose copies do not land within a bounded wait makes the step return
+ * MHD_ERR_TIMEOUT.  That
  * give-up path waits a second bounded time for the copies still in flight;
  * should that wait also run out, the block exits with bulk copies possibly
  * still writing its shared memory, which is unsafe -- the option stays off
  * by default, and no test drives either wait to its limit. */
 int mhd_set_update_path(mhd_ctx *ctx, int tma);
-/* 1 if the split stage's update is TMA-staged, 0 if not. */
+/* Precision diagnostic of the plain form: with on = 1 the arithmetic stays
+ * FP64 but every stage stores U and V rounded to FP32, as a form with FP32
+ * state must -- a run of it (from an FP32-rounded start) measures the error
+ * that FP32 storage alone causes, the floor of MHD_PREC_FP32's error against
+ * the plain form.  MHD_ERR_ARG on a precision-form context. */
+int mhd_set_state_rounding(mhd_ctx *ctx, int on);
+/* The split stage's update path set by mhd_set_update_path (0, 1 or 2). */
 int mhd_update_path(const mhd_ctx *ctx);
 /* Kernels this context has launched since creation. */
 long long mhd_launch_count(const mhd_ctx *ctx);

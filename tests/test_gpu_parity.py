@@ -122,23 +122,32 @@ def test_dt_guard(M):
 
 
 def test_precision_form_against_fp64(M, P):
-    """FP32 state/fluxes with FP64 repair vs the FP64 oracle after 10 steps:
-    every conserved variable within 1e-4 relative L1 on this small grid."""
+    """FP32 state/fluxes with FP64 repair vs the FP64 oracle after 10 steps, on
+    all nine conserved variables: within 2x the FP32-storage floor (the plain
+    form's FP64 arithmetic with U and V rounded to FP32 after every stage,
+    from the rounded start), and within 1e-4 relative L1 on the order-one
+    components."""
     grid, params, U, V = make_case(M, "rk3_minmod_hlld", (32, 32, 32))
     o = oracle_for(M, P, grid, params)
     Uo, Vo, _, _ = run_oracle(o, U, V, 10)
-    params32 = M.default_params(**{k: v for k, v in params.as_dict().items() if k != "precision"},
-                                precision="fp32")
-    d = M.Disc(grid, params32)
-    d.upload(U, V)
-    t = 0.0
-    for _ in range(10):
-        rc, t, dt, ch, cnt = d.step(t)
-        assert rc == 0
-    Ug, Vg = d.download()
-    err = rel_l1(Ug, Uo)
-    # psi starts at 0 and stays tiny: measure it against the field scale instead
-    err[8] = np.abs(Ug[8] - Uo[8]).sum() / max(np.abs(Uo[4:7]).sum(), 1e-300)
-    assert np.all(err[:8] < 1e-4), err
-    d.close()
     o.close()
+    base = {k: v for k, v in params.as_dict().items() if k != "precision"}
+
+    def gpu(prec, U0, V0, round_state=False):
+        d = M.Disc(grid, M.default_params(precision=prec, **base))
+        if round_state:
+            d.set_state_rounding(True)
+        d.upload(U0, V0)
+        t = 0.0
+        for _ in range(10):
+            rc, t, dt, ch, cnt = d.step(t)
+            assert rc == 0
+        Ug, _ = d.download()
+        d.close()
+        return Ug
+
+    U32, V32 = U.astype(np.float32).astype(np.float64), V.astype(np.float32).astype(np.float64)
+    floor = rel_l1(gpu("fp64", U32, V32, round_state=True), Uo)
+    err = rel_l1(gpu("fp32", U, V), Uo)
+    assert np.all(err <= np.maximum(2.0 * floor, 1e-7)), (err, floor)
+    assert np.all(err[[0, 1, 2, 5, 7]] < 1e-4), err

@@ -17,8 +17,9 @@ pytestmark = pytest.mark.gpu
 
 # (nr, nphi, nz): one tile; ragged tiles in k (70 = 2x32 + 6) and j; runs in r
 SHAPES = [(20, 12, 14), (40, 24, 70)]
-# (fused, tj, seg): 1 = one fused stage kernel, 2 = z fluxes fused into the update, 0 = split
-STAGE = [(1, 7, 32), (1, 7, 5), (1, 7, 1), (2, 7, 32), (0, 7, 32)]
+# (fused, tj, seg): 1 = one fused stage kernel, 2 = z fluxes fused into the update, 0 = split,
+# 3 = split kernels pipelined over seg slabs of i planes (uneven slabs, one slab, more slabs than planes)
+STAGE = [(1, 7, 32), (1, 7, 5), (1, 7, 1), (2, 7, 32), (0, 7, 32), (3, 7, 3), (3, 7, 1), (3, 7, 64)]
 
 
 def same(a, b):
@@ -100,6 +101,6 @@ def test_fp32_run_graph_follows_shape(M):
 def test_stage_shape_rejects_bad_arguments(M):
     grid, params, U, V = make_case(M, "rk3_minmod_hlld", (20, 12, 14))
     d = M.Disc(grid, params)
-    for bad in [(3, 7, 32), (1, 3, 32), (1, 7, 0)]:
+    for bad in [(4, 7, 32), (1, 3, 32), (1, 7, 0), (3, 7, 65), (3, 7, 0)]:
         assert M.lib().mhd_set_stage_shape(d.h, *bad) == M.MHD_ERR_ARG
     d.close()

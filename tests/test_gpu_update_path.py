@@ -109,3 +109,20 @@ def test_staged_update_refused_where_unavailable(M):
         rc, t, *_ = d.step(t)
         assert rc == 0
     d.close()
+
+
+@pytest.mark.parametrize("dims", SHAPES + [(13, 8, 13)])
+def test_prefetching_update_is_bitwise_the_loads(M, dims):
+    """Path 2: the same thread loads, with each block prefetching the block one
+    wave ahead into L2 -- the same arithmetic, so the same bits."""
+    grid, params, U, V = make_case(M, "rk3_mc_hlld_grav_cool", dims)
+    p32 = fp32(M, params)
+    Up, Vp, logp, path = run_path(M, grid, p32, U, V, 5, 2)
+    assert path == 2
+    Ul, Vl, logl, _ = run_path(M, grid, p32, U, V, 5, 0)
+    assert logp == logl
+    assert np.array_equal(Up, Ul) and np.array_equal(Vp, Vl)
+    d = M.Disc(grid, params)           # plain FP64 form: not offered
+    with pytest.raises(M.MhdError):
+        d.set_update_path(2)
+    d.close()
