@@ -685,7 +685,8 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     a.zghost = ctx->fused == 0;   /* the split update fills the interior columns' k-plane ghosts */
     /* path 2: each update block prefetches the block one wave ahead into L2
      * (8 resident blocks of 128 threads per SM in the precision form) */
-    a.prefetch = ctx->upd_tma == 2 ? 8 * ctx->nsm : 0;
+    a.prefetch = (ctx->upd_tma & 2) ? 8 * ctx->nsm : 0;
+    a.wfromu = (ctx->upd_tma & 4) ? 1 : 0;
     if (ctx->fused == 1) {
         LAUNCH(PK_STAGE, launch_stage(ctx->G, a, ctx->stage_tj, ctx->stage_seg, ctx->st));
     } else if (ctx->fused == 3) {
@@ -1219,7 +1220,8 @@ extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
 
 extern "C" int mhd_set_update_path(mhd_ctx *ctx, int tma)
 {
-    if (!ctx || tma < 0 || tma > 2 || (tma == 1 && !ctx->maps) || (tma == 2 && !ctx->fp32)) return MHD_ERR_ARG;
+    if (!ctx || tma < 0 || tma > 6 || tma == 3 || tma == 5 || (tma == 1 && !ctx->maps) || (tma > 1 && !ctx->fp32))
+        return MHD_ERR_ARG;
     ctx->upd_tma = tma;
     if (ctx->graph_ready) {
         CK(cudaStreamSynchronize(ctx->st));

@@ -320,8 +320,16 @@ __device__ __forceinline__ int update_core(const Geom &G, const StageArgs<T> &a,
     const T dt = Scal<T>::dt(sc), psicoef = Scal<T>::psi(sc);
     const int kind = a.kind;
     T W[9], S[9], u[9];
+    if (sizeof(T) == 4 && a.wfromu) {
+        /* the stage's input primitives are UtoV of its input state U^(k)
+         * (U^n in the first stage, U1 after it): recomputed, not loaded */
 #pragma unroll
-    for (int m = 0; m < 9; m++) W[m] = in.v(m);
+        for (int m = 0; m < 9; m++) u[m] = (kind == 0) ? in.un(m) : in.u1(m);
+        utov<T>(G, i, u, W);
+    } else {
+#pragma unroll
+        for (int m = 0; m < 9; m++) W[m] = in.v(m);
+    }
     source_at<T>(G, *sc, a.trig, a.trigf, i, j, k, W, S);
 #pragma unroll
     for (int m = 0; m < 9; m++) {

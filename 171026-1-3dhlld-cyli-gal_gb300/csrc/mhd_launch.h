@@ -52,6 +52,7 @@ struct StageArgs {
     int zghost = 0;        /* 1: the update fills the k-plane ghosts of interior (i,j) columns */
     int prefetch = 0;      /* update: blocks ahead whose streamed inputs each block prefetches into L2 (0: none) */
     int ibeg = 1, iend = 0;  /* update: the planes i in [ibeg, iend) it covers (iend 0: through ixmax-2) */
+    int wfromu = 0;        /* update (precision form): the cell's primitives from UtoV of U^(k), not loaded */
 };
 
 #define MHD_DECLARE_LAUNCHERS(T)                                                                             \

@@ -126,3 +126,20 @@ def test_prefetching_update_is_bitwise_the_loads(M, dims):
     with pytest.raises(M.MhdError):
         d.set_update_path(2)
     d.close()
+
+
+@pytest.mark.parametrize("path", [4, 6])
+@pytest.mark.parametrize("variant", ["rk3_mc_hlld_grav_cool", "rk2_mc_hll_grav_cool"])
+def test_primitives_from_state_match_loads(M, variant, path):
+    """Paths 4 and 6: the update forms the cell's input primitives as UtoV of
+    its input state U^(k) instead of loading V (which holds UtoV of the same
+    state, corrected by Check where a floor fired), 6 with the L2 prefetch of
+    path 2.  Same values up to rounding where floors fired."""
+    grid, params, U, V = make_case(M, variant, (40, 24, 70))
+    p32 = fp32(M, params)
+    Uw, Vw, logw, p = run_path(M, grid, p32, U, V, 5, path)
+    assert p == path
+    Ul, Vl, logl, _ = run_path(M, grid, p32, U, V, 5, 0)
+    assert [c for _, _, c in logw] == [c for _, _, c in logl], "floor counters"
+    assert np.all(field_scaled_err(grid, Uw, Ul) <= 1e-6)
+    assert np.all(field_scaled_err(grid, Vw, Vl) <= 1e-5)
