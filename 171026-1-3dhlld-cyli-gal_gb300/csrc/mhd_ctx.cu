@@ -682,7 +682,7 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     a.Vout = (T *)vnext_ptr(ctx); a.Uraw = (T *)ctx->Uraw;
     a.sc = ctx->d_sc; a.trig = ctx->d_trig; a.trigf = ctx->d_trigf; a.kind = kind; a.last = last; a.counters = counters;
     a.Vinit = Vinit;
-    a.zghost = ctx->fused == 0;   /* the split update fills the interior columns' k-plane ghosts */
+    a.zghost = ctx->fused == 0 || ctx->fused == 3;   /* the split updates fill the interior columns' k-plane ghosts */
     /* path 2: each update block prefetches the block one wave ahead into L2
      * (8 resident blocks of 128 threads per SM in the precision form) */
     a.prefetch = (ctx->upd_tma & 2) ? 8 * ctx->nsm : 0;

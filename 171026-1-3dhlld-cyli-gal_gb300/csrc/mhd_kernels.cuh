@@ -336,16 +336,9 @@ __device__ __forceinline__ int update_core(const Geom &G, const StageArgs<T> &a,
         T un = in.un(m), u1 = (kind == 0) ? T(0) : in.u1(m);
         T v;
         if (sizeof(T) == 4) {
-            /* precision form: one rounding per stage (stage_combine) */
-            float eun = 0.0f, eu1 = 0.0f;
-            if (m == 8) {   /* GLMSourceSolver on U and U1, product residuals kept */
-                const float pn = (float)psicoef * (float)un, p1 = (float)psicoef * (float)u1;
-                eun = fmaf((float)psicoef, (float)un, -pn);
-                eu1 = fmaf((float)psicoef, (float)u1, -p1);
-                un = pn;
-                u1 = p1;
-            }
-            v = (T)stage_combine(kind, (float)un, (float)u1, (float)dt, (float)div[m], (float)S[m], eun, eu1);
+            /* precision form: the combination in increment form (stage_combine) */
+            if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
+            v = (T)stage_combine(kind, (float)un, (float)u1, (float)dt, (float)div[m], (float)S[m]);
         } else {
             if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
             if (kind == 0) v = un - dt * div[m] + dt * S[m];

@@ -397,25 +397,31 @@ def batch_bench(args):
            "discs_stopped_by_dt_guard": stopped, "clocks": clocks,
            "sizes": [list(dims) for dims, _, _ in wl]}
     if args.batch_check:
-        errs = []
+        errs, twin, floor = [], [], []
         b = M.Batch(grids, params)
         for d, (U, V) in enumerate(states):
             b.upload(d, U, V)
+        mode = args.batch_check_mode
+        if mode == "tuned":
+            b.set_mode(best[4], best[0] if best[4] == 2 else 0)
+        else:
+            mm, _, arg = mode.partition(":")
+            b.set_mode(int(mm), int(arg or 0))
         _, st32 = b.step(args.batch_check, np.zeros(n))
-        stopped64 = 0
-        twin = []
+        stopped64 = {"fp64": 0, "twin": 0, "floor": 0}
 
-        def run64(d, U, V):
-            nonlocal stopped64
+        def run64(d, U, V, what):
             pd = params[d].as_dict()
             pd.pop("precision")
             s64 = M.Disc(grids[d], M.default_params(precision="fp64", **pd))
+            if what == "floor":
+                s64.set_state_rounding(True)
             s64.upload(U, V)
             tt = 0.0
             for _ in range(args.batch_check):
                 rc, tt, *_ = s64.step(tt)
                 if rc != 0:          # dt guard: this disc stops, as in the batch
-                    stopped64 += 1
+                    stopped64[what] += 1
                     break
             Uo, _ = s64.download()
             s64.close()
@@ -426,22 +432,29 @@ def batch_bench(args):
 
         for d in range(n):
             U, V = states[d]
-            U64 = run64(d, U, V)
+            U64 = run64(d, U, V, "fp64")
             Ub, _ = b.download(d)
             errs.append(rel(Ub, U64))
-            # the plain form from the FP32-rounded start: the divergence floor
-            Ut = run64(d, U.astype(np.float32).astype(np.float64), V.astype(np.float32).astype(np.float64))
-            twin.append(rel(Ut, U64))
+            # the plain form from the FP32-rounded start (twin), and with the
+            # state also rounded to FP32 after every stage (the storage floor)
+            U32, V32 = U.astype(np.float32).astype(np.float64), V.astype(np.float32).astype(np.float64)
+            twin.append(rel(run64(d, U32, V32, "twin"), U64))
+            floor.append(rel(run64(d, U32, V32, "floor"), U64))
         b.close()
-        errs = np.array(errs)
-        twin = np.array(twin)
+        errs, twin, floor = np.array(errs), np.array(twin), np.array(floor)
         names = ["rho", "m_r", "r*m_phi", "m_z", "B_r", "B_phi", "B_z", "E", "psi"]
-        out["fp64_check"] = {"steps": args.batch_check,
-                             "stopped_by_dt_guard": {"batch": int(np.count_nonzero(st32)), "fp64_and_twin": stopped64},
+        ratio = errs / np.maximum(floor, 1e-300)
+        out["fp64_check"] = {"steps": args.batch_check, "mode": mode,
+                             "stopped_by_dt_guard": {"batch": int(np.count_nonzero(st32)), **stopped64},
                              "max_over_discs_rel_l1": dict(zip(names, errs.max(axis=0).tolist())),
                              "median_over_discs_rel_l1": dict(zip(names, np.median(errs, axis=0).tolist())),
+                             "storage_floor_median_over_discs_rel_l1": dict(zip(names, np.median(floor, axis=0).tolist())),
+                             "storage_floor_max_over_discs_rel_l1": dict(zip(names, floor.max(axis=0).tolist())),
                              "fp64_twin_median_over_discs_rel_l1": dict(zip(names, np.median(twin, axis=0).tolist())),
-                             "fp64_twin_max_over_discs_rel_l1": dict(zip(names, twin.max(axis=0).tolist()))}
+                             "fp64_twin_max_over_discs_rel_l1": dict(zip(names, twin.max(axis=0).tolist())),
+                             "err_over_floor_median": dict(zip(names, np.median(ratio, axis=0).tolist())),
+                             "err_over_floor_max": dict(zip(names, ratio.max(axis=0).tolist())),
+                             "worst_disc_by_rho": int(np.argmax(errs[:, 0]))}
     print(json.dumps(out))
     return 0
 
@@ -608,6 +621,8 @@ def main():
     ap.add_argument("--monitor-forms", default="fp32", help="fp32, fp64 or fp32,fp64")
     ap.add_argument("--monitor-solvers", default="hlld,hll")
     ap.add_argument("--batch-check", type=int, default=0, metavar="NSTEPS")
+    ap.add_argument("--batch-check-mode", default="tuned",
+                    help="batch mode of the checked run: tuned, 0 (persistent), 1 (phased), 2:B (disc graph, B branches)")
     args = ap.parse_args()
     if args.precision_report:
         return precision_report(args)
