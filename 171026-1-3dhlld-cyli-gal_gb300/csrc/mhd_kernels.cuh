@@ -320,6 +320,7 @@ __device__ __forceinline__ int update_core(const Geom &G, const StageArgs<T> &a,
     const T dt = Scal<T>::dt(sc), psicoef = Scal<T>::psi(sc);
     const int kind = a.kind;
     T W[9], S[9], u[9];
+    const StageCoef kc = stage_coef(kind);
     if (sizeof(T) == 4 && a.wfromu) {
         /* the stage's input primitives are UtoV of its input state U^(k)
          * (U^n in the first stage, U1 after it): recomputed, not loaded */
@@ -336,9 +337,9 @@ __device__ __forceinline__ int update_core(const Geom &G, const StageArgs<T> &a,
         T un = in.un(m), u1 = (kind == 0) ? T(0) : in.u1(m);
         T v;
         if (sizeof(T) == 4) {
-            /* precision form: the combination in increment form (stage_combine) */
+            /* precision form: the combination in increment form (stage_combine_k) */
             if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
-            v = (T)stage_combine(kind, (float)un, (float)u1, (float)dt, (float)div[m], (float)S[m]);
+            v = (T)stage_combine_k(kc, (float)un, (float)u1, (float)dt, (float)div[m], (float)S[m]);
         } else {
             if (m == 8) { un = psicoef * un; u1 = psicoef * u1; }   /* GLMSourceSolver on U and U1 */
             if (kind == 0) v = un - dt * div[m] + dt * S[m];

@@ -45,7 +45,9 @@ def test_batch_matches_single_disc_runs(M):
         ts = s.run(5, 0.0)
         Us, _ = s.download()
         Ub, _ = b.download(d)
-        assert abs(ts - t[d]) <= 1e-12 * ts, d
+        # the default (persistent) mode's flux kernels compute the same faces
+        # with other FP32 roundings: dt follows the state to the form's precision
+        assert abs(ts - t[d]) <= 1e-7 * ts, d
         err = rel_l1(Ub[:8], Us[:8])
         # B_r, B_z start at zero in these discs: against the field scale
         bscale = np.abs(Us[4:7]).sum()
@@ -58,9 +60,11 @@ def test_batch_matches_single_disc_runs(M):
 
 def test_batch_against_fp64(M):
     """Every disc of the batch against its own plain FP64 run after 4 steps, on
-    all nine conserved variables: within 2x that disc's FP32-storage floor
+    all nine conserved variables: within 3x that disc's FP32-storage floor
     (FP64 arithmetic, U and V rounded to FP32 after every stage, rounded
-    start) and within 1e-4 on the order-one components."""
+    start) plus 1e-7 -- after 4 steps both are single realisations of
+    rounding noise a few times 1e-7 -- and within 1e-4 on the order-one
+    components."""
     cases = make_discs(M)
     b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
     for d, (g, p, U, V) in enumerate(cases):
@@ -86,7 +90,7 @@ def test_batch_against_fp64(M):
         Ufl = run64(g, pd, U.astype(np.float32).astype(np.float64), V.astype(np.float32).astype(np.float64), True)
         Ub, _ = b.download(d)
         err, floor = rel_l1(Ub, U64), rel_l1(Ufl, U64)
-        assert np.all(err <= np.maximum(2.0 * floor, 1e-7)), (d, err, floor)
+        assert np.all(err <= 3.0 * floor + 1e-7), (d, err, floor)
         assert np.all(err[[0, 1, 2, 5, 7]] <= 1e-4), (d, err)
     b.close()
 
@@ -148,7 +152,8 @@ def test_batch_plain_fp64_is_bitwise_per_disc(M):
 def test_batch_modes_match_single_disc_runs(M, mode, arg):
     """Each mode against the discs stepped alone (mhd_run).  The disc graph
     runs the single-disc kernels themselves: bit for bit; the persistent and
-    phased kernels to the precision form's 1e-6."""
+    phased kernels (one thread per face, other FP32 roundings) to the
+    precision form's 1e-6, and dt to 1e-7."""
     cases = make_discs(M)
     b = M.Batch([c[0] for c in cases], [c[1] for c in cases])
     b.set_mode(mode, arg)
@@ -163,7 +168,7 @@ def test_batch_modes_match_single_disc_runs(M, mode, arg):
         ts = s.run(5, 0.0)
         Us, _ = s.download()
         Ub, _ = b.download(d)
-        assert abs(ts - t[d]) <= 1e-12 * ts, d
+        assert abs(ts - t[d]) <= (0.0 if mode == 2 else 1e-7) * ts, d
         if mode == 2:
             assert ts == t[d] and np.array_equal(Ub, Us), d
         else:
