@@ -10,19 +10,24 @@
  *                   amplitude and dt guard (setdt.h:84-89, main.c:331,
  *                   tvdrungekutta.h:33-34, spiralgravity.h:41-42)
  *   arm phase       cos/sin per (i,j) of every disc with gravity
- *   3 RK stages     ONE persistent launch per stage: blocks take tiles from a
- *                   global queue ordered [flux tiles of all discs][update
- *                   tiles][ghost tiles]; an update tile waits (bounded spin)
- *                   until its disc's flux tiles are done, a ghost tile until
- *                   its disc's update tiles are done.  Every tile a block waits
- *                   for was taken earlier by a running block, so the waits end.
+ *   3 RK stages     ONE persistent launch per stage: blocks take work items
+ *                   from a global queue ordered in waves -- the r, phi and z
+ *                   flux items of slab w (a slab = sl planes in r) of every
+ *                   disc, then the update items of slab w - lag -- and the
+ *                   ghost items last.  An update item waits (bounded spin)
+ *                   until the flux items of its slab and the slab below are
+ *                   done, a ghost item until its disc's update items are.
+ *                   Every item a block waits for was taken earlier by a
+ *                   running block, so the waits end.  The items run the
+ *                   single-disc kernels' code (marched r/phi faces, the
+ *                   z walk, the update, the ghost fill).
  *   advance         t += dt per disc whose guard did not fire
  *
- * captured as one CUDA graph per primitive-buffer parity.  Tile shape (r x phi
- * x z cells per tile), threads per block and the register cap (launch
- * bounds) are chosen by mhd_batch_tune(), which times candidates on the live
- * state and restores it.  The halo is read through L1 from global memory, so
- * its depth is the stencil's (2 cells) for every tile shape.
+ * captured as one CUDA graph per primitive-buffer parity.  Slab depth (the r
+ * extent of the items), queue lag and the register cap (launch bounds) are
+ * chosen by mhd_batch_tune(), which times candidates on the live state and
+ * restores it.  The halo is read through L1 from global memory, so its depth
+ * is the stencil's (2 cells) for every slab depth.
  *
  * Two other modes are tuner candidates: phased (one launch per stage phase
  * over all discs) and the disc graph (each disc's own single-disc step, the
@@ -57,36 +62,30 @@ struct DiscDev {
     float *trigf;
     MaxLoc *part;
     int *counters;          /* [3 stages][3] */
-    Box fbox[3], ubox;      /* flux face boxes per direction, interior box */
-    int ft[3][3];           /* flux tiles along i, j, k per direction */
-    int ut[3];              /* update tiles along i, j, k */
-    int nflux, nupd, nghost, ndt;
+    Box fbox[3], ubox;      /* flux face boxes per direction, interior box (phased mode) */
+    int ndt;
+    /* persistent stage: the disc cut into slabs of sl interior planes in r;
+     * work items are laid out kx lanes along k by ky rows (kx * ky = 128) */
+    int sl, ns, kx, ky, tk, tjr, nruns, nghost;
+    int foff;               /* this disc's slab counters in the stage's readiness array */
+    int stall;              /* test hook: slab 0 waits for one flux item more than exist */
     double cfl, minminlength, dtmin, psifac, tausp, epssp0, omdiff, armnum;
     int gravity;
 };
 
+/* Persistent-stage configurations the tuner times: slab depth in r planes
+ * (the r extent of a work item and the unit of readiness), queue lag (slabs
+ * of flux items enqueued ahead of an update slab), and the register cap: the
+ * kernel instantiated for 5 or 4 resident blocks of 128 threads per SM (at
+ * most 102 or 128 registers per thread). */
 struct TileCfg {
-    int ti, tj, tk, bt, variant;
+    int sl, lag, minb;
 };
-
-/* candidate configurations, each a compiled variant: tile ti x tj x tk cells
- * (512-1024 per queue item, so the queue head sees few atomics), bt threads,
- * register cap 65536/(bt*minblocks) */
-#define MHD_BATCH_VARIANTS(X)      \
-    X(0, 128, 4, 1, 4, 128)        \
-    X(1, 256, 2, 1, 4, 128)        \
-    X(2, 256, 2, 1, 8, 128)        \
-    X(3, 256, 2, 2, 4, 128)        \
-    X(4, 128, 4, 1, 8, 64)         \
-    X(5, 256, 3, 1, 4, 256)        \
-    X(6, 512, 1, 1, 4, 128)        \
-    X(7, 128, 6, 1, 4, 128)
-static const TileCfg CANDIDATES[] = {
-#define MHD_CAND(V, BT, MB, TI, TJ, TK) {TI, TJ, TK, BT, V},
-    MHD_BATCH_VARIANTS(MHD_CAND)
-#undef MHD_CAND
-};
+static const TileCfg CANDIDATES[] = {{16, 1, 5}, {16, 2, 5}, {8, 1, 5}, {8, 2, 5},
+                                     {32, 1, 5}, {16, 1, 4}, {16, 2, 4}, {8, 2, 4}};
 static const int NCAND = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
+#define MHD_ZROWS 16    /* (i,j) rows of a z item: 4 per warp */
+#define MHD_UPLANES 4   /* planes of an update item */
 #define MHD_SPIN_LIMIT (1 << 24)
 
 __device__ __forceinline__ void add_counts(int a, int b, int c, int *counters)
@@ -130,80 +129,179 @@ __device__ __forceinline__ void load_geom(Geom &sG, const Geom &G)
     __syncthreads();
 }
 
-template <int BT, int MINB, int TI, int TJ, int TK>
-__global__ void __launch_bounds__(BT, MINB)
-batch_stage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ tiles, int ntiles, int *head,
-                   int *done, int ndisc, int *err, int spin, int kind, int last, int parity, int stage)
+/* item kinds of the persistent stage, and the item counts of slab s of a disc */
+enum { IT_R = 0, IT_P = 1, IT_Z = 2, IT_U = 3, IT_G = 4 };
+
+__host__ __device__ __forceinline__ int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+__host__ __device__ __forceinline__ void slab_items(const DiscDev &D, int s, int &nR, int &nP, int &nZ, int &nU)
 {
-    __shared__ int s_t, s_ok;
+    const int ni = D.G.ixmax - 2, nj = D.G.jymax - 2;
+    const int planes = min(D.sl, ni - s * D.sl);
+    nR = D.tjr * D.tk;                                    /* (j,k) line tiles, all faces of the slab */
+    nP = cdiv(planes, D.ky) * D.tk * D.nruns;             /* (i,k) line tiles x runs of 16 phi faces */
+    nZ = cdiv(planes * nj, MHD_ZROWS);                    /* (i,j) rows, 16 per item */
+    nU = cdiv(planes, MHD_UPLANES) * D.tjr * D.tk;        /* cell tiles, MHD_UPLANES planes each */
+}
+
+/* The work items, each a function of its own (not inlined) so the kernel's
+ * register allocation is not the union of all five paths.  Slab s covers the
+ * interior planes [a0, b0). */
+__device__ __forceinline__ void slab_planes(const Geom &G, const DiscDev &D, int slab, int &a0, int &b0)
+{
+    a0 = 1 + slab * D.sl;
+    b0 = min(a0 + D.sl, G.ixmax - 1);
+}
+
+/* r faces of the slab (slab 0 also face 0) on one (j,k) line per thread */
+__device__ __noinline__ void item_r(const Geom &G, const DiscDev &D, const float *V, int slab, int local)
+{
+    int a0, b0;
+    slab_planes(G, D, slab, a0, b0);
+    const int tx = threadIdx.x % D.kx, ty = threadIdx.x / D.kx;
+    const int j = 1 + (local / D.tk) * D.ky + ty, k = 1 + (local % D.tk) * D.kx + tx;
+    if (j <= G.jymax - 2 && k <= G.kzmax - 2) march_run<float, 0, false>(G, V, D.Vinit, D.sc, D.F, j, k, slab == 0 ? 0 : a0, b0);
+}
+
+/* a run of 16 phi faces on one (i,k) line per thread */
+__device__ __noinline__ void item_p(const Geom &G, const DiscDev &D, const float *V, int slab, int local)
+{
+    int a0, b0;
+    slab_planes(G, D, slab, a0, b0);
+    const int tx = threadIdx.x % D.kx, ty = threadIdx.x / D.kx;
+    const int run = local % D.nruns, rest = local / D.nruns;
+    const int i = a0 + (rest / D.tk) * D.ky + ty, k = 1 + (rest % D.tk) * D.kx + tx;
+    const int nf = G.jymax - 1;
+    if (i < b0 && k <= G.kzmax - 2) march_run<float, 1, false>(G, V, D.Vinit, D.sc, D.Gf, i, k, 16 * run, min(16 * run + 16, nf));
+}
+
+/* MHD_ZROWS (i,j) rows: per row the two boundary z faces, then the walk */
+__device__ __noinline__ void item_z(const Geom &G, const DiscDev &D, const float *V, int slab, int local)
+{
+    int a0, b0;
+    slab_planes(G, D, slab, a0, b0);
+    const int nj = G.jymax - 2, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int rr = 0; rr < MHD_ZROWS / 4; rr++) {
+        const int row = local * MHD_ZROWS + w * (MHD_ZROWS / 4) + rr;
+        if (row >= (b0 - a0) * nj) break;   /* warp-uniform */
+        const int i = a0 + row / nj, j = 1 + row % nj;
+        if (lane < 2) flux_face<float, 2, false>(G, V, D.Vinit, D.sc, D.H, i, j, lane == 0 ? 0 : G.kzmax - 2);
+        zwalk_row<float, false>(G, V, D.sc, D.H, i, j, 1, G.kzmax - 2);
+    }
+}
+
+/* update of MHD_UPLANES planes of a (j,k) tile */
+__device__ __noinline__ void item_u(const Geom &G, const StageArgs<float> &a, const DiscDev &D, int slab, int local)
+{
+    int a0, b0;
+    slab_planes(G, D, slab, a0, b0);
+    const int tx = threadIdx.x % D.kx, ty = threadIdx.x / D.kx;
+    const int tkk = local % D.tk, rest = local / D.tk;
+    const int j = 1 + (rest % D.tjr) * D.ky + ty, k = 1 + tkk * D.kx + tx, tp = rest / D.tjr;
+    int c0 = 0, c1 = 0, c2 = 0;
+    if (j <= G.jymax - 2 && k <= G.kzmax - 2)
+        for (int ii = 0; ii < MHD_UPLANES; ii++) {
+            const int i = a0 + tp * MHD_UPLANES + ii;
+            if (i >= b0) break;
+            const int f = update_cell<float>(G, a, i, j, k);
+            c0 += f & 1; c1 += (f >> 1) & 1; c2 += (f >> 2) & 1;
+        }
+    add_counts(c0, c1, c2, a.counters);
+}
+
+/* 128 ghost cells (the rim of the k planes, the i and j planes) */
+__device__ __noinline__ void item_g(const Geom &G, const StageArgs<float> &a, int local)
+{
+    const unsigned g = (unsigned)local * 128u + threadIdx.x;
+    int f = 0;
+    if (g < ghost_count(G, 1)) f = ghost_cell<float>(G, a, g);
+    add_counts(f & 1, (f >> 1) & 1, (f >> 2) & 1, a.counters);
+}
+
+/* One persistent launch per RK stage over all discs.  Blocks take work items
+ * from a queue ordered in waves: the flux items (r, phi, z) of slab w of every
+ * disc, then the update items of slab w - lag.  An update item of slab s
+ * waits -- a bounded spin, then the error flag -- until every flux item of
+ * slabs s and s-1 of its disc is done (its lower r face belongs to slab s-1),
+ * a ghost item until every update item of its disc is.  Everything an item
+ * waits for sits earlier in the queue and was taken by a block already
+ * running, so the waits end.  The items run the single-disc kernels' code:
+ * march_run (r and phi faces, each cell reconstructed once per direction),
+ * zwalk_row plus the two boundary z faces, update_cell, ghost_cell. */
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB)
+batch_pstage_kernel(const DiscDev *__restrict__ discs, const uint2 *__restrict__ items, int nitems, int *head,
+                    int *fdone, int *udone, int *err, int spin, int kind, int last, int parity, int stage)
+{
+    __shared__ int s_t, s_ok, s_d;
     __shared__ Geom sG;
+    __shared__ StageArgs<float> sA;   /* an update or ghost item's arguments, read from shared memory */
+    if (threadIdx.x == 0) s_d = -1;
+    const int tid = threadIdx.x;
     for (;;) {
-        if (threadIdx.x == 0) s_t = atomicAdd(head, 1);
+        if (tid == 0) s_t = atomicAdd(head, 1);
         __syncthreads();
         const int t = s_t;
-        if (t >= ntiles) return;
-        const uint2 e = tiles[t];
-        const int d = (int)e.x, code = (int)(e.y >> 28), local = (int)(e.y & 0x0fffffffu);
+        if (t >= nitems) return;
+        const uint2 e = items[t];
+        const int d = (int)e.x, type = (int)(e.y >> 28), slab = (int)((e.y >> 18) & 0x3ffu),
+                  local = (int)(e.y & 0x3ffffu);
         const DiscDev &D = discs[d];
-        load_geom(sG, D.G);
-        if (threadIdx.x == 0) {
+        if (s_d != d) {   /* block-uniform */
+            __syncthreads();
+            const int *src = (const int *)&D.G;
+            int *dst = (int *)&sG;
+            for (int w = tid; w < (int)(sizeof(Geom) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+            __syncthreads();
+            if (tid == 0) s_d = d;
+        }
+        if (tid == 0) {
             int ok = 1;
-            if (code == 3) ok = wait_at_least(&done[d], D.nflux, err, spin);
-            else if (code == 4) ok = wait_at_least(&done[ndisc + d], D.nupd, err, spin);
+            if (type == IT_U) {
+                int nR, nP, nZ, nU;
+                slab_items(D, slab, nR, nP, nZ, nU);
+                ok = wait_at_least(&fdone[D.foff + slab], nR + nP + nZ + (slab == 0 ? D.stall : 0), err, spin);
+                if (ok && slab > 0) {
+                    slab_items(D, slab - 1, nR, nP, nZ, nU);
+                    ok = wait_at_least(&fdone[D.foff + slab - 1], nR + nP + nZ + (slab == 1 ? D.stall : 0), err, spin);
+                }
+            } else if (type == IT_G) {
+                int tot = 0;
+                for (int q = 0; q < D.ns; q++) {
+                    int nR, nP, nZ, nU;
+                    slab_items(D, q, nR, nP, nZ, nU);
+                    tot += nU;
+                }
+                ok = wait_at_least(&udone[d], tot, err, spin);
+            }
             s_ok = ok;
         }
         __syncthreads();
         if (!s_ok) return;
         const bool live = !D.sc->dtbad;
         const float *V = parity ? D.Vb : D.Va;
-        if (live && code < 3) {
-            const Box &b = D.fbox[code];
-            const int ntk = D.ft[code][2], ntj = D.ft[code][1];
-            const int tk = local % ntk, tj = (local / ntk) % ntj, tii = local / (ntk * ntj);
-            constexpr int n = TI * TJ * TK;
-            float *Fd = code == 0 ? D.F : code == 1 ? D.Gf : D.H;
-            for (int c = threadIdx.x; c < n; c += BT) {
-                const int kk = c % TK, jj = (c / TK) % TJ, ii = c / (TK * TJ);
-                const int i = b.i0 + tii * TI + ii, j = b.j0 + tj * TJ + jj, k = b.k0 + tk * TK + kk;
-                if (i >= b.i1 || j >= b.j1 || k >= b.k1) continue;
-                if (code == 0) flux_face<float, 0, false>(sG, V, D.Vinit, D.sc, Fd, i, j, k);
-                else if (code == 1) flux_face<float, 1, false>(sG, V, D.Vinit, D.sc, Fd, i, j, k);
-                else flux_face<float, 2, false>(sG, V, D.Vinit, D.sc, Fd, i, j, k);
+        if (live && type == IT_R) item_r(sG, D, V, slab, local);
+        else if (live && type == IT_P) item_p(sG, D, V, slab, local);
+        else if (live && type == IT_Z) item_z(sG, D, V, slab, local);
+        else if (live) {
+            if (tid == 0) {
+                StageArgs<float> a;
+                a.V = V; a.F = D.F; a.G = D.Gf; a.H = D.H; a.Un = D.U; a.U1 = D.U1;
+                a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw;
+                a.Vinit = D.Vinit; a.sc = D.sc; a.trig = D.trig; a.trigf = D.trigf; a.kind = kind; a.last = last;
+                a.counters = D.counters + 3 * stage;
+                a.zghost = 1;   /* the update fills the interior columns' k-plane ghosts, the ghost items the rest */
+                sA = a;
             }
-        } else if (live) {
-            StageArgs<float> a;
-            a.V = V; a.F = D.F; a.G = D.Gf; a.H = D.H; a.Un = D.U; a.U1 = D.U1;
-            a.Uinit = D.Uinit; a.rhofloor = D.rhofloor; a.Vout = parity ? D.Va : D.Vb; a.Uraw = D.Uraw; a.Vinit = D.Vinit;
-            a.sc = D.sc; a.trig = D.trig; a.trigf = D.trigf; a.kind = kind; a.last = last;
-            a.counters = D.counters + 3 * stage;
-            int c0 = 0, c1 = 0, c2 = 0;
-            if (code == 3) {
-                const Box &b = D.ubox;
-                const int ntk = D.ut[2], ntj = D.ut[1];
-                const int tk = local % ntk, tj = (local / ntk) % ntj, tii = local / (ntk * ntj);
-                constexpr int n = TI * TJ * TK;
-                for (int c = threadIdx.x; c < n; c += BT) {
-                    const int kk = c % TK, jj = (c / TK) % TJ, ii = c / (TK * TJ);
-                    const int i = b.i0 + tii * TI + ii, j = b.j0 + tj * TJ + jj, k = b.k0 + tk * TK + kk;
-                    if (i >= b.i1 || j >= b.j1 || k >= b.k1) continue;
-                    int f = update_cell<float>(sG, a, i, j, k);
-                    c0 += f & 1; c1 += (f >> 1) & 1; c2 += (f >> 2) & 1;
-                }
-            } else {
-                const unsigned ng = ghost_count(sG);
-                const unsigned g0 = (unsigned)local * (unsigned)(4 * BT);
-                for (unsigned g = g0 + threadIdx.x; g < g0 + 4 * BT && g < ng; g += BT) {
-                    int f = ghost_cell<float>(sG, a, g);
-                    c0 += f & 1; c1 += (f >> 1) & 1; c2 += (f >> 2) & 1;
-                }
-            }
-            add_counts(c0, c1, c2, a.counters);
+            __syncthreads();
+            if (type == IT_U) item_u(sG, sA, D, slab, local);
+            else item_g(sG, sA, local);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             __threadfence();
-            if (code < 3) atomicAdd(&done[d], 1);
-            else if (code == 3) atomicAdd(&done[ndisc + d], 1);
+            if (type <= IT_Z) atomicAdd(&fdone[D.foff + slab], 1);
+            else if (type == IT_U) atomicAdd(&udone[d], 1);
         }
     }
 }
@@ -396,9 +494,11 @@ struct mhd_batch {
     DiscDev *dd;
     TileCfg cfg;
     int nblk_stage;
-    /* tile tables */
+    /* work items of the persistent stage, in queue order, and the CFL row tiles */
     uint2 *dtiles, *ddt;
     int ntiles, ndt_tiles, rows_per_tile;
+    int nslabs;                 /* slab counters of all discs (readiness array length) */
+    int qlen;                   /* ints per stage in dqueue: head, slab counters, per-disc update counts */
     int phased;                 /* 1: one launch per phase, 0: one persistent launch per stage */
     int discgraph;              /* 1: every disc's own device-resident step, all in one graph */
     int nbranch;                /*    on this many parallel stream branches */
@@ -409,7 +509,7 @@ struct mhd_batch {
     int nph[4];
     uint2 *dghost;
     int nghost_tiles;
-    int *dqueue;    /* [3 stages]: head ; then done [3 stages][2*n] */
+    int *dqueue;    /* [3 stages][qlen] */
     int *derr;
     int *dcnt;      /* per disc [3][3] */
     cudaGraphExec_t gx[2];
@@ -427,45 +527,66 @@ struct mhd_batch {
 
 static int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
-/* tile tables for a configuration */
+/* the persistent stage's work items for a configuration, in queue order */
 static int build_tiles(mhd_batch *b, TileCfg c)
 {
-    std::vector<uint2> tl;
     const int n = b->n;
+    int foff = 0, maxns = 0;
     for (int d = 0; d < n; d++) {
         DiscDev &D = b->hd[d];
-        D.nflux = 0;
-        for (int dir = 0; dir < 3; dir++) {
-            const Box &bx = D.fbox[dir];
-            D.ft[dir][0] = ceil_div(bx.i1 - bx.i0, c.ti);
-            D.ft[dir][1] = ceil_div(bx.j1 - bx.j0, c.tj);
-            D.ft[dir][2] = ceil_div(bx.k1 - bx.k0, c.tk);
-            int nt = D.ft[dir][0] * D.ft[dir][1] * D.ft[dir][2];
-            for (int l = 0; l < nt; l++) tl.push_back(make_uint2(d, ((unsigned)dir << 28) | (unsigned)l));
-            D.nflux += nt;
+        const int ni = D.G.ixmax - 2, nj = D.G.jymax - 2, nk = D.G.kzmax - 2;
+        D.sl = c.sl;
+        D.ns = cdiv(ni, c.sl);
+        D.kx = 32 * cdiv(nk < 128 ? nk : 128, 32);
+        if (D.kx == 96) D.kx = 128;   /* kx * ky = 128 */
+        D.ky = 128 / D.kx;
+        D.tk = cdiv(nk, D.kx);
+        D.tjr = cdiv(nj, D.ky);
+        D.nruns = cdiv(nj + 1, 16);
+        D.nghost = cdiv((int)ghost_count(D.G, 1), 128);
+        D.foff = foff;
+        D.stall = d == b->stall_disc ? 1 : 0;
+        foff += D.ns;
+        maxns = std::max(maxns, D.ns);
+    }
+    std::vector<uint2> tl;
+    auto push = [&](int d, int type, int slab, int cnt) {
+        for (int l = 0; l < cnt; l++)
+            tl.push_back(make_uint2(d, ((unsigned)type << 28) | ((unsigned)slab << 18) | (unsigned)l));
+    };
+    for (int w = 0; w < maxns + c.lag; w++) {
+        for (int d = 0; d < n; d++) {
+            const DiscDev &D = b->hd[d];
+            if (w >= D.ns) continue;
+            int nR, nP, nZ, nU;
+            slab_items(D, w, nR, nP, nZ, nU);
+            push(d, IT_R, w, nR);
+            push(d, IT_P, w, nP);
+            push(d, IT_Z, w, nZ);
         }
-        if (d == b->stall_disc) D.nflux += 1;   /* the update tiles' wait can then only time out */
+        const int u = w - c.lag;
+        for (int d = 0; d < n && u >= 0; d++) {
+            const DiscDev &D = b->hd[d];
+            if (u >= D.ns) continue;
+            int nR, nP, nZ, nU;
+            slab_items(D, u, nR, nP, nZ, nU);
+            push(d, IT_U, u, nU);
+        }
     }
-    for (int d = 0; d < n; d++) {
-        DiscDev &D = b->hd[d];
-        D.ut[0] = ceil_div(D.ubox.i1 - D.ubox.i0, c.ti);
-        D.ut[1] = ceil_div(D.ubox.j1 - D.ubox.j0, c.tj);
-        D.ut[2] = ceil_div(D.ubox.k1 - D.ubox.k0, c.tk);
-        D.nupd = D.ut[0] * D.ut[1] * D.ut[2];
-        for (int l = 0; l < D.nupd; l++) tl.push_back(make_uint2(d, (3u << 28) | (unsigned)l));
-    }
-    for (int d = 0; d < n; d++) {
-        DiscDev &D = b->hd[d];
-        long long ng = 2LL * D.G.ixmax * D.G.jymax + 2LL * D.G.ixmax * (D.G.kzmax - 2) +
-                       2LL * (D.G.jymax - 2) * (D.G.kzmax - 2);
-        D.nghost = (int)((ng + 4 * c.bt - 1) / (4 * c.bt));
-        for (int l = 0; l < D.nghost; l++) tl.push_back(make_uint2(d, (4u << 28) | (unsigned)l));
-    }
+    for (int d = 0; d < n; d++) push(d, IT_G, 0, b->hd[d].nghost);
     if (b->dtiles) cudaFree(b->dtiles);
     b->dtiles = NULL;
     b->ntiles = (int)tl.size();
     BCK(cudaMalloc((void **)&b->dtiles, tl.size() * sizeof(uint2)));
     BCK(cudaMemcpy(b->dtiles, tl.data(), tl.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    b->nslabs = foff;
+    const int qlen = 1 + foff + n;
+    if (qlen != b->qlen) {
+        if (b->dqueue) cudaFree(b->dqueue);
+        b->dqueue = NULL;
+        BCK(cudaMalloc((void **)&b->dqueue, 3 * (size_t)qlen * sizeof(int)));
+        b->qlen = qlen;
+    }
     BCK(cudaMemcpy(b->dd, b->hd.data(), n * sizeof(DiscDev), cudaMemcpyHostToDevice));
     b->cfg = c;
     return MHD_OK;
@@ -476,32 +597,22 @@ static int stage_blocks(TileCfg c)
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    switch (c.variant) {
-#define MHD_OCC(V, BT, MB, TI, TJ, TK)                                                                    \
-    case V: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_stage_kernel<BT, MB, TI, TJ, TK>, BT, 0); \
-        break;
-        MHD_BATCH_VARIANTS(MHD_OCC)
-#undef MHD_OCC
-    default: break;
-    }
+    if (c.minb == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_pstage_kernel<4>, 128, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_pstage_kernel<5>, 128, 0);
     if (per < 1) per = 1;
     return sms * per;
 }
 
-static cudaError_t launch_stage(mhd_batch *b, int *head, int *done, int kind, int last, int parity, int stage)
+static cudaError_t launch_stage(mhd_batch *b, int *q, int kind, int last, int parity, int stage)
 {
-    int nb = b->nblk_stage;
-    switch (b->cfg.variant) {
-#define MHD_LAUNCH(V, BT, MB, TI, TJ, TK)                                                                  \
-    case V:                                                                                                \
-        batch_stage_kernel<BT, MB, TI, TJ, TK><<<nb, BT, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, done, \
-                                                                     b->n, b->derr, b->spin_limit, kind, last,    \
-                                                                     parity, stage);                              \
-        break;
-        MHD_BATCH_VARIANTS(MHD_LAUNCH)
-#undef MHD_LAUNCH
-    default: return cudaErrorInvalidValue;
-    }
+    const int nb = b->nblk_stage;
+    int *head = q, *fdone = q + 1, *udone = q + 1 + b->nslabs;
+    if (b->cfg.minb == 4)
+        batch_pstage_kernel<4><<<nb, 128, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, fdone, udone, b->derr,
+                                                      b->spin_limit, kind, last, parity, stage);
+    else
+        batch_pstage_kernel<5><<<nb, 128, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, fdone, udone, b->derr,
+                                                      b->spin_limit, kind, last, parity, stage);
     return cudaGetLastError();
 }
 
@@ -573,9 +684,9 @@ static int enqueue_batch_step(mhd_batch *b, int parity)
             BCK(cudaGetLastError());
             b->launches += 5;
         } else {
-            int *q = b->dqueue + s * (1 + 2 * n);
-            BCK(cudaMemsetAsync(q, 0, (1 + 2 * n) * sizeof(int), b->st));
-            BCK(launch_stage(b, q, q + 1, kind, last, par, s));
+            int *q = b->dqueue + (size_t)s * b->qlen;
+            BCK(cudaMemsetAsync(q, 0, b->qlen * sizeof(int), b->st));
+            BCK(launch_stage(b, q, kind, last, par, s));
             b->launches++;
         }
         par ^= 1;
@@ -660,7 +771,6 @@ static int setup_persistent(mhd_batch *b)
     BCK(cudaMalloc((void **)&b->ddt, dt.size() * sizeof(uint2)));
     BCK(cudaMemcpy(b->ddt, dt.data(), dt.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     BCK(cudaMalloc((void **)&b->dd, n * sizeof(DiscDev)));
-    BCK(cudaMalloc((void **)&b->dqueue, 3 * (1 + 2 * n) * sizeof(int)));
     BCK(cudaMalloc((void **)&b->derr, sizeof(int)));
     BCK(cudaMemset(b->derr, 0, sizeof(int)));
     BCK(cudaMalloc((void **)&b->dcnt, 9 * n * sizeof(int)));
@@ -957,10 +1067,10 @@ extern "C" int mhd_batch_tune(mhd_batch *b, int *best)
     } else if (b->phased) {
         best[0] = 1; best[1] = 1; best[2] = 128; best[3] = 128; best[4] = 1;
     } else {
-        best[0] = CANDIDATES[best_i].ti;
-        best[1] = CANDIDATES[best_i].tj;
-        best[2] = CANDIDATES[best_i].tk;
-        best[3] = CANDIDATES[best_i].bt;
+        best[0] = CANDIDATES[best_i].sl;
+        best[1] = CANDIDATES[best_i].lag;
+        best[2] = 65536 / (128 * CANDIDATES[best_i].minb);
+        best[3] = 128;
         best[4] = 0;
     }
     return MHD_OK;

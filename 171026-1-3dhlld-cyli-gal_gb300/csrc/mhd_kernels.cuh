@@ -83,18 +83,17 @@ __device__ __forceinline__ void store_face(const Geom &G, T *__restrict__ F, int
  * fixed fills); a run starts with the left slot of its first interior cell.  Whole blocks share
  * the run, so the edge faces never diverge inside a warp.  Same operations
  * per state as face_states, so the plain form keeps its bits. */
-template <typename T, int DIR, int MR, bool REFLAYOUT>
-__global__ void __launch_bounds__(128)
-march_flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
-                  T *__restrict__ F, Box b)
+/* One thread's run of faces [f0, fe) along r (DIR 0) or phi (DIR 1) on the
+ * line t (j for r, i for phi) at height k: the body of march_flux_kernel,
+ * also the r and phi work items of the batched form's persistent stage. */
+template <typename T, int DIR, bool REFLAYOUT>
+__device__ __forceinline__ void march_run(const Geom &G, const T *__restrict__ V, const T *__restrict__ Vinit,
+                                          const StepScalars *__restrict__ sc, T *__restrict__ F, int t, int k,
+                                          int f0, int fe)
 {
-    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int t = (DIR == 0 ? b.j0 : b.i0) + blockIdx.y * blockDim.y + threadIdx.y;
-    int f0 = (DIR == 0 ? b.i0 : b.j0) + blockIdx.z * MR;
-    const int fe = min(f0 + MR, DIR == 0 ? b.i1 : b.j1);
-    if (k >= b.k1 || t >= (DIR == 0 ? b.j1 : b.i1)) return;
     const int N = (DIR == 0 ? G.ixmax : G.jymax) - 2;
     const T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
+    if (f0 >= fe) return;
     if (f0 == 0) {
         flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, DIR == 0 ? 0 : t, DIR == 0 ? t : 0, k);
         f0 = 1;
@@ -118,6 +117,29 @@ march_flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, 
     if (fe > N) flux_face<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, DIR == 0 ? N : t, DIR == 0 ? t : N, k);
 }
 
+/* Faces along r (DIR 0) or phi (DIR 1), one thread marching over a run of MR
+ * consecutive faces f of one (j,k) or (i,k) line.  Face f takes the left slot
+ * of cell f and the right slot of cell f+1 (1 <= f <= N-1, N = nmax-2), so
+ * each step reconstructs cell f+1 once, both slots (cell_slots), uses its
+ * right slot now and carries its left slot to face f+1: one cell pass per
+ * face where a thread per face (flux_face) makes two slot passes.  The first
+ * and last face of the direction keep flux_face (their periodic / free /
+ * fixed fills); a run starts with the left slot of its first interior cell.  Whole blocks share
+ * the run, so the edge faces never diverge inside a warp.  Same operations
+ * per state as face_states, so the plain form keeps its bits. */
+template <typename T, int DIR, int MR, bool REFLAYOUT>
+__global__ void __launch_bounds__(128)
+march_flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
+                  T *__restrict__ F, Box b)
+{
+    const int k = b.k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (DIR == 0 ? b.j0 : b.i0) + blockIdx.y * blockDim.y + threadIdx.y;
+    const int f0 = (DIR == 0 ? b.i0 : b.j0) + blockIdx.z * MR;
+    const int fe = min(f0 + MR, DIR == 0 ? b.i1 : b.j1);
+    if (k >= b.k1 || t >= (DIR == 0 ? b.j1 : b.i1)) return;
+    march_run<T, DIR, REFLAYOUT>(G, V, Vinit, sc, F, t, k, f0, fe);
+}
+
 /* Interior z faces (1 .. kzmax-3 within the box), one warp walking each
  * (i,j) row in chunks of 32 cells: lane l reconstructs cell c = c0 + l once,
  * both slots (cell_slots), and forms face c-1 from its own right slot and the
@@ -127,17 +149,14 @@ march_flux_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, 
  * coalesced along k.  Same operations per state as face_states, so the
  * plain form keeps its bits.  FP32: held to 64 registers (8 blocks per SM),
  * 1.48 against 1.56 ms at 78 registers for 512x512x256. */
+/* One warp's walk of the interior z faces flo .. fhi-1 of row (i, j): the
+ * body of zwalk_flux_kernel, also the z work items of the batched form's
+ * persistent stage.  Warp-uniform arguments. */
 template <typename T, bool REFLAYOUT>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1)
-zwalk_flux_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc, T *__restrict__ F, Box b)
+__device__ __forceinline__ void zwalk_row(const Geom &G, const T *__restrict__ V, const StepScalars *__restrict__ sc,
+                                          T *__restrict__ F, int i, int j, int flo, int fhi)
 {
     const int lane = threadIdx.x & 31;
-    const int nj = b.j1 - b.j0;
-    const long long nrow = (long long)(b.i1 - b.i0) * nj;
-    const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (row >= nrow) return;   /* a whole warp */
-    const int i = b.i0 + (int)(row / nj), j = b.j0 + (int)(row % nj);
-    const int flo = max(b.k0, 1), fhi = min(b.k1, G.kzmax - 2);   /* faces flo .. fhi-1, cells flo .. fhi */
     const T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
     T carry[9];
 #pragma unroll
@@ -164,6 +183,28 @@ zwalk_flux_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict
             store_face<T, REFLAYOUT>(G, F, i, j, c - 1, Fo);
         }
     }
+}
+
+/* Interior z faces (1 .. kzmax-3 within the box), one warp walking each
+ * (i,j) row in chunks of 32 cells: lane l reconstructs cell c = c0 + l once,
+ * both slots (cell_slots), and forms face c-1 from its own right slot and the
+ * left slot of cell c-1, which the lane below holds (a shuffle; lane 0 takes
+ * lane 31's from the previous chunk).  One cell pass per face where the
+ * four-cell stencil of interior_states makes two slot passes; loads stay
+ * coalesced along k.  Same operations per state as face_states, so the
+ * plain form keeps its bits.  FP32: held to 64 registers (8 blocks per SM),
+ * 1.48 against 1.56 ms at 78 registers for 512x512x256. */
+template <typename T, bool REFLAYOUT>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1)
+zwalk_flux_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc, T *__restrict__ F, Box b)
+{
+    const int nj = b.j1 - b.j0;
+    const long long nrow = (long long)(b.i1 - b.i0) * nj;
+    const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= nrow) return;   /* a whole warp */
+    const int i = b.i0 + (int)(row / nj), j = b.j0 + (int)(row % nj);
+    const int flo = max(b.k0, 1), fhi = min(b.k1, G.kzmax - 2);   /* faces flo .. fhi-1, cells flo .. fhi */
+    zwalk_row<T, REFLAYOUT>(G, V, sc, F, i, j, flo, fhi);
 }
 
 /* The two z boundary faces of each (i,j) column (face 0 and face kzmax-2,

@@ -367,6 +367,19 @@ def batch_bench(args):
     w0 = time.perf_counter()
     best = b.tune()
     tune_s = time.perf_counter() - w0
+    # every mode the tuner chooses among, timed on its own over a few steps
+    mode_ms = {}
+    for name, mode, arg in ([("persistent_%d" % c, 0, c) for c in range(8)] +
+                            [("phased", 1, 0)] + [("disc_graph_%d" % k, 2, k) for k in (4, 16)]):
+        bm = M.Batch(grids, params)
+        for d, (U, V) in enumerate(states):
+            bm.upload(d, U, V)
+        bm.set_mode(mode, arg)
+        tm, _ = bm.step(2, np.zeros(n))
+        w0 = time.perf_counter()
+        bm.step(5, tm)
+        mode_ms[name] = (time.perf_counter() - w0) / 5 * 1e3
+        bm.close()
     t, st = b.step(args.warmup, t)
     sampler = ClockSampler()
     sampler.start()
@@ -392,8 +405,10 @@ def batch_bench(args):
            "value": zones * args.steps / wall, "unit": "zone-updates/s", "ms_per_step": wall / args.steps * 1e3,
            "sequential_single_disc": {"value": zones * args.steps / seq_wall, "ms_per_step": seq_wall / args.steps * 1e3},
            "tuned": ({"mode": "disc_graph", "branches": best[0], "tune_seconds": tune_s} if best[4] == 2 else
-                     {"tile_r": best[0], "tile_phi": best[1], "tile_z": best[2], "threads": best[3],
-                      "mode": "phased" if best[4] == 1 else "persistent", "tune_seconds": tune_s}),
+                     {"mode": "phased", "tune_seconds": tune_s} if best[4] == 1 else
+                     {"mode": "persistent", "slab_planes": best[0], "queue_lag": best[1],
+                      "registers_per_thread": best[2], "threads": best[3], "tune_seconds": tune_s}),
+           "modes_ms_per_step": mode_ms,
            "discs_stopped_by_dt_guard": stopped, "clocks": clocks,
            "sizes": [list(dims) for dims, _, _ in wl]}
     if args.batch_check:

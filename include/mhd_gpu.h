@@ -312,24 +312,30 @@ int mhd_batch_download(mhd_batch *b, int disc, double *U, double *V);
 /* nsteps steps of every disc, each with its own dt; t[n] advance in place;
  * status[n] = 0 or MHD_ERR_DT for a disc whose dt guard fired (that disc then
  * stops advancing).  The whole step is one CUDA graph launch.  Precision form:
- * by default one persistent launch per RK stage over a tile queue of all
- * discs; mhd_batch_tune() may pick the phased or disc-graph mode instead.
- * Plain form: the discs' mhd_step() one after another. */
+ * by default one persistent launch per RK stage over a work queue of all
+ * discs (r, phi and z flux items and update items per slab of r planes,
+ * ghost items; an update slab waits, bounded, for the flux items of its slab
+ * and the one below); mhd_batch_tune() may pick the phased or disc-graph
+ * mode instead.  Plain form: the discs' mhd_step() one after another. */
 int mhd_batch_step(mhd_batch *b, int nsteps, double *t, int *status);
 /* Times candidate configurations on the current state and keeps the fastest;
  * the state is restored afterwards.  Candidates: the persistent per-stage
- * launch with each compiled tile shape / block size / register cap (mode 0),
- * the phased form -- one launch per stage phase over all discs (mode 1) --
- * and the disc graph -- every disc's own single-disc step, the discs dealt to
- * 2, 4, 8 or 16 parallel stream branches of one graph (mode 2).
- * best[5] = {tile_i, tile_j, tile_k, threads, mode}; mode 2: {branches, 0, 0, 0, 2}. */
+ * launch with each of 8 configurations (mode 0: slab depth 8, 16 or 32 r
+ * planes, queue lag 1 or 2 slabs, register cap 102 or 128 per thread), the
+ * phased form -- one launch per stage phase over all discs (mode 1) -- and
+ * the disc graph -- every disc's own single-disc step, the discs dealt to 2,
+ * 4, 8 or 16 parallel stream branches of one graph (mode 2).
+ * best[5] = {slab planes, queue lag, registers per thread, threads, 0} for
+ * mode 0; {1, 1, 128, 128, 1} for mode 1; {branches, 0, 0, 0, 2} for mode 2. */
 int mhd_batch_tune(mhd_batch *b, int *best);
-/* Pick the precision form's batch mode directly: 0 persistent with compiled
- * tile candidate arg, 1 phased, 2 disc graph on arg branches (1..64). */
+/* Pick the precision form's batch mode directly: 0 persistent with
+ * configuration arg (0..7, the tuner's order), 1 phased, 2 disc graph on arg
+ * branches (1..64). */
 int mhd_batch_set_mode(mhd_batch *b, int mode, int arg);
-/* Test hook for the persistent mode's bounded waits (an update tile waits,
- * with an iteration limit, for its disc's flux tiles): with disc >= 0 that
- * disc's flux count is set one above what the stage produces and the limit
+/* Test hook for the persistent mode's bounded waits (an update item waits,
+ * with an iteration limit, for its slab's flux items): with disc >= 0 the
+ * flux count that disc's first slab waits for is set one above what the
+ * stage produces and the limit
  * to spin_limit, so the next step's wait runs out -- no fault, no hang -- and
  * mhd_batch_step returns MHD_ERR_TIMEOUT (the state of that step is then
  * undefined: upload again).  disc = -1 restores normal operation.  Selects
