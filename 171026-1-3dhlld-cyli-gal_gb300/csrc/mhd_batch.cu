@@ -81,7 +81,7 @@ struct DiscDev {
 struct TileCfg {
     int sl, lag, minb;
 };
-static const TileCfg CANDIDATES[] = {{16, 1, 5}, {16, 2, 5}, {8, 1, 5}, {8, 2, 5},
+static const TileCfg CANDIDATES[] = {{16, 1, 5}, {16, 2, 5}, {8, 1, 8}, {16, 1, 8},
                                      {32, 1, 5}, {16, 1, 4}, {16, 2, 4}, {8, 2, 4}};
 static const int NCAND = sizeof(CANDIDATES) / sizeof(CANDIDATES[0]);
 #define MHD_ZROWS 16    /* (i,j) rows of a z item: 4 per warp */
@@ -598,6 +598,7 @@ static int stage_blocks(TileCfg c)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (c.minb == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_pstage_kernel<4>, 128, 0);
+    else if (c.minb == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_pstage_kernel<8>, 128, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_pstage_kernel<5>, 128, 0);
     if (per < 1) per = 1;
     return sms * per;
@@ -609,6 +610,9 @@ static cudaError_t launch_stage(mhd_batch *b, int *q, int kind, int last, int pa
     int *head = q, *fdone = q + 1, *udone = q + 1 + b->nslabs;
     if (b->cfg.minb == 4)
         batch_pstage_kernel<4><<<nb, 128, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, fdone, udone, b->derr,
+                                                      b->spin_limit, kind, last, parity, stage);
+    else if (b->cfg.minb == 8)
+        batch_pstage_kernel<8><<<nb, 128, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, fdone, udone, b->derr,
                                                       b->spin_limit, kind, last, parity, stage);
     else
         batch_pstage_kernel<5><<<nb, 128, 0, b->st>>>(b->dd, b->dtiles, b->ntiles, head, fdone, udone, b->derr,
