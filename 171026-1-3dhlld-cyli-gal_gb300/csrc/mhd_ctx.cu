@@ -559,12 +559,18 @@ extern "C" int mhd_upload(mhd_ctx *ctx, const double *U, const double *V, const 
 
 extern "C" int mhd_upload_state(mhd_ctx *ctx, const double *U, const double *V)
 {
-    if (!ctx || !U || !V) return MHD_ERR_ARG;
+    if (!ctx || !U) return MHD_ERR_ARG;
     if (!ctx->uploaded) return MHD_ERR_STATE;
     int rc;
     if ((rc = put_state(ctx, ctx->U, U, 9 * ctx->nc))) return rc;
     ctx->vcur = 0;
-    if ((rc = put_state(ctx, ctx->Va, V, 9 * ctx->nc))) return rc;
+    if (V) {
+        if ((rc = put_state(ctx, ctx->Va, V, 9 * ctx->nc))) return rc;
+    } else if (ctx->fp32) {   /* V = UtoV(U) on the device */
+        LAUNCH(PK_CVT, launch_derive_v(ctx->G, (const float *)ctx->U, (float *)ctx->Va, ctx->st));
+    } else {
+        LAUNCH(PK_CVT, launch_derive_v(ctx->G, (const double *)ctx->U, (double *)ctx->Va, ctx->st));
+    }
     CK(cudaStreamSynchronize(ctx->st));   /* the caller's arrays are free again on return */
     return MHD_OK;
 }

@@ -1070,6 +1070,23 @@ __global__ void cvt_to_f64(const T *__restrict__ src, double *__restrict__ dst, 
         dst[t] = (double)src[t];
 }
 
+/* V = UtoV(U) at every cell, ghosts included (utov.h:24-68, no floors): the
+ * primitives of a state uploaded without them */
+template <typename T>
+__global__ void __launch_bounds__(256) derive_v_kernel(Geom G, const T *__restrict__ U, T *__restrict__ V)
+{
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < G.nc;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q / ((long long)G.jymax * G.kzmax));
+        T u[9], w[9];
+#pragma unroll
+        for (int m = 0; m < 9; m++) u[m] = U[m * G.nc + q];
+        utov<T>(G, i, u, w);
+#pragma unroll
+        for (int m = 0; m < 9; m++) V[m * G.nc + q] = w[m];
+    }
+}
+
 /* source term probe (SpiralGravityCooling over all cells) */
 template <typename T>
 __global__ void source_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc,
@@ -1305,6 +1322,13 @@ cudaError_t launch_cvt_t(const double *src, T *dst, long long n, cudaStream_t st
 }
 
 template <typename T>
+cudaError_t launch_derive_v_t(const Geom &G, const T *U, T *V, cudaStream_t st)
+{
+    derive_v_kernel<T><<<(unsigned)(4 * sm_count()), 256, 0, st>>>(G, U, V);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream_t st)
 {
     cvt_to_f64<T><<<1024, 256, 0, st>>>(src, dst, n);
@@ -1377,6 +1401,10 @@ cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream
     cudaError_t launch_cvt_back(const T *src, double *dst, long long n, cudaStream_t st)                     \
     {                                                                                                        \
         return launch_cvt_back_t<T>(src, dst, n, st);                                                        \
+    }                                                                                                        \
+    cudaError_t launch_derive_v(const Geom &G, const T *U, T *V, cudaStream_t st)                           \
+    {                                                                                                        \
+        return launch_derive_v_t<T>(G, U, V, st);                                                            \
     }                                                                                                        \
     }
 

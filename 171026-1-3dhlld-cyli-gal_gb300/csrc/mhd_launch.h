@@ -75,7 +75,8 @@ struct StageArgs {
     cudaError_t launch_source(const Geom &G, const T *V, const StepScalars *sc, const double *trig,          \
                               const float *trigf, double *S, cudaStream_t st);                               \
     cudaError_t launch_cvt(const double *src, T *dst, long long n, cudaStream_t st);                         \
-    cudaError_t launch_cvt_back(const T *src, double *dst, long long n, cudaStream_t st);
+    cudaError_t launch_cvt_back(const T *src, double *dst, long long n, cudaStream_t st);                    \
+    cudaError_t launch_derive_v(const Geom &G, const T *U, T *V, cudaStream_t st);
 
 MHD_DECLARE_LAUNCHERS(double)
 MHD_DECLARE_LAUNCHERS(float)

@@ -226,7 +226,13 @@ int mhd_diagnostics(mhd_ctx *ctx, mhd_diag *d);
 /* The CUDA stream the context launches on (as a cudaStream_t). */
 void *mhd_stream(mhd_ctx *ctx);
 /* Upload only the evolving state U, V (same layout as mhd_upload); the
- * initial arrays and floors from the last mhd_upload stay. */
+ * initial arrays and floors from the last mhd_upload stay.  V = NULL: the
+ * primitives are formed on the device as UtoV(U) (utov.h:24-68) at every cell,
+ * which halves the bytes a host that keeps only the conserved state moves
+ * (with mhd_download(ctx, U, NULL) on the way back).  Where Check's floors
+ * fired in the step that produced U, UtoV(U) differs from the V that step
+ * stored by rounding, so the plain form is then no longer bit-identical to a
+ * reference run that kept V. */
 int mhd_upload_state(mhd_ctx *ctx, const double *U, const double *V);
 
 /* Asynchronous BinaryOutput of the context's current V: the state is copied

@@ -113,7 +113,8 @@ def test_default_line_has_the_contract_keys(bench_with_stand_in, monkeypatch, ca
     assert d["config"]["workload"].startswith("disc5") and d["config"]["zones"] == zones
     assert d["gpu_launches"] == 4 * 21
     e = d["e2e"]
-    assert e["unit"] == d["unit"] and e["h2d_bytes_per_step"] == e["d2h_bytes_per_step"] == 2 * 9 * 26 * 18 * 22 * 8
+    assert e["unit"] == d["unit"] and e["h2d_bytes_per_step"] == e["d2h_bytes_per_step"] == 9 * 26 * 18 * 22 * 8
+    assert e["with_v"]["h2d_bytes_per_step"] == 2 * 9 * 26 * 18 * 22 * 8
     assert e["ms_per_step"] == pytest.approx(4.0) and e["value"] == pytest.approx(zones / 4e-3)
     r = d["roofline"]
     assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["kernel"] == "update"
@@ -131,10 +132,10 @@ def test_default_line_has_the_contract_keys(bench_with_stand_in, monkeypatch, ca
     assert kr["flux_r"]["bytes_per_launch"] == 25 * 16 * 20 * 18 * 4
     assert kr["setdt"]["bytes_per_launch"] == 14 * 16 * 20 * 8 * 4
     f = d["fp64"]
-    assert f["e2e"]["unit"] == d["unit"] and f["e2e"]["h2d_bytes_per_step"] == e["h2d_bytes_per_step"]
+    assert f["e2e"]["unit"] == d["unit"] and f["e2e"]["h2d_bytes_per_step"] == e["with_v"]["h2d_bytes_per_step"]
     assert f["kernels"]["update"]["bytes_per_launch"] == zones * 70 * 8
     hl = d["host_link"]
-    assert hl["bytes"] == e["h2d_bytes_per_step"] and hl["h2d_gbs"] == pytest.approx(hl["bytes"] / 1e-3 / 1e9)
+    assert hl["bytes"] == e["with_v"]["h2d_bytes_per_step"] and hl["h2d_gbs"] == pytest.approx(hl["bytes"] / 1e-3 / 1e9)
     st = d["step_traffic"]
     assert st["fused_minimum_gbs"] == pytest.approx(300 * zones / 2e-3 / 1e9)
 

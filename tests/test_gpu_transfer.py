@@ -5,7 +5,7 @@ context stays usable afterwards."""
 import numpy as np
 import pytest
 
-from mhdcase import make_case
+from mhdcase import make_case, rel_l1
 
 pytestmark = pytest.mark.gpu
 
@@ -51,3 +51,32 @@ def test_pinned_and_staged_transfers_agree(M, pin):
     assert t2 == t
     assert np.array_equal(Uo, Ur) and np.array_equal(Vo, Vr)
     d.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_state_upload_without_primitives(M, prec):
+    """mhd_upload_state(U, NULL) forms V = UtoV(U) on the device; a host that
+    keeps only the conserved state moves half the bytes.  After a step from
+    U alone the state matches the step from U and V: to 1e-12 relative L1 in
+    the plain form (UtoV(U) is the initial condition's V to rounding) and to
+    1e-6 in the precision form; the V read back is the one the device
+    formed."""
+    grid, params, U, V = make_case(M, "rk3_minmod_hlld", (24, 16, 20))
+    d = M.Disc(grid, M.default_params(**{k: v for k, v in params.as_dict().items() if k != "precision"},
+                                      precision=prec))
+    d.upload(U, V)
+    d.upload_state(U, None)
+    _, Vd = d.download()
+    # the device's UtoV of the uploaded U: V to rounding
+    assert np.all(rel_l1(Vd, V) <= (1e-14 if prec == "fp64" else 1e-6))
+    rc, t1, *_ = d.step(0.0)
+    Ua = np.zeros_like(U)
+    d.download_into(Ua, None)
+    d.upload_state(U, V)
+    rc, t2, *_ = d.step(0.0)
+    Ub, _ = d.download()
+    d.close()
+    err = rel_l1(Ua, Ub)
+    err[[3, 4, 6, 8]] = [np.abs(Ua[m] - Ub[m]).sum() / max(np.abs(Ub[4:7]).sum(), 1e-300) for m in (3, 4, 6, 8)]
+    assert np.all(err <= (1e-12 if prec == "fp64" else 1e-6)), err
+    assert abs(t1 - t2) <= 1e-9 * t2
