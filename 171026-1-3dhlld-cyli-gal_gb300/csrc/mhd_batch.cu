@@ -829,7 +829,8 @@ extern "C" int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *
     int fp32 = params[0].precision == MHD_PREC_FP32;
     b->nst = params[0].scheme == MHD_SCHEME_RK2 ? 2 : 3;
     for (int i = 0; i < n; i++) {
-        if ((params[i].precision == MHD_PREC_FP32) != fp32 || params[i].scheme != params[0].scheme) {
+        if ((params[i].precision == MHD_PREC_FP32) != fp32 || params[i].precision == MHD_PREC_FP32X2 ||
+            params[i].scheme != params[0].scheme) {
             mhd_batch_destroy(b);
             return MHD_ERR_ARG;   /* one precision and one RK scheme per batch */
         }

@@ -166,7 +166,8 @@ static void free_all(mhd_ctx *ctx)
     if (ctx->writer.joinable()) ctx->writer.join();
     void *dev[] = {ctx->dtab, ctx->ftab, ctx->U, ctx->U1, ctx->Va, ctx->Vb, ctx->Uinit, ctx->Vinit,
                    ctx->rhofloor, ctx->F, ctx->Gf, ctx->H, ctx->Uraw, ctx->d_sc, ctx->d_trig, ctx->d_trigf,
-                   ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run, ctx->d_snap};
+                   ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run, ctx->d_snap, ctx->Ulo, ctx->U1lo,
+                   ctx->Urawlo, ctx->Zs};
     if (ctx->h_snap) cudaFreeHost(ctx->h_snap);
     for (int q = 0; q < NSTAGE; q++) {
         if (ctx->ev_cp[q]) cudaEventDestroy(ctx->ev_cp[q]);
@@ -253,7 +254,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     int rc = check_grid(g);
     if (rc) return rc;
     if (p->limiter < 0 || p->limiter > 3 || p->solver < 0 || p->solver > 1 || p->source < 0 || p->source > 3 ||
-        (p->scheme != MHD_SCHEME_RK2 && p->scheme != MHD_SCHEME_RK3) || p->precision < 0 || p->precision > 1)
+        (p->scheme != MHD_SCHEME_RK2 && p->scheme != MHD_SCHEME_RK3) || p->precision < 0 || p->precision > 2)
         return MHD_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return MHD_ERR_NODEV;
@@ -274,7 +275,8 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     ctx->ixmax = g->ix + 2; ctx->jymax = g->jy + 2; ctx->kzmax = g->kz + 2;
     ctx->irin = g->irin;
     ctx->nc = (long long)ctx->ixmax * ctx->jymax * ctx->kzmax;
-    ctx->fp32 = p->precision == MHD_PREC_FP32;
+    ctx->fp32 = p->precision == MHD_PREC_FP32 || p->precision == MHD_PREC_FP32X2;
+    ctx->pair = p->precision == MHD_PREC_FP32X2;
     ctx->esz = ctx->fp32 ? sizeof(float) : sizeof(double);
     const int ixmax = ctx->ixmax, jymax = ctx->jymax, kzmax = ctx->kzmax;
     const long long nc = ctx->nc;
@@ -354,6 +356,8 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     size_t o_z = put(g->z, kzmax);
     size_t o_dvol = put(dvol.data(), nik);
     std::vector<float> TF(T.begin(), T.end());   /* FP32 copies at the same offsets */
+    const size_t o_oxlo = TF.size();              /* the low words of the FP32 1/x (pair-state form) */
+    for (int i = 0; i < ixmax; i++) TF.push_back((float)(g->oneox[i] - (double)(float)g->oneox[i]));
 
 #define CKC(call)                                  \
     do {                                           \
@@ -389,6 +393,7 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
     G.spA = D + o_spA; G.spS = D + o_spS; G.spQ = D + o_spQ; G.spR = D + o_spR;
     G.spC1 = D + o_C1; G.spC2 = D + o_C2; G.spD = D + o_D; G.spL = D + o_L; G.y = D + o_y; G.z = D + o_z;
     G.dvol = D + o_dvol; G.dy = g->dy;
+    G.oneoxlo = Fd + o_oxlo;
     G.graxif = Fd + o_grax; G.spAf = Fd + o_spA; G.spSf = Fd + o_spS; G.spQf = Fd + o_spQ; G.spRf = Fd + o_spR;
     G.spC1f = Fd + o_C1; G.spC2f = Fd + o_C2; G.spDf = Fd + o_D; G.zf = Fd + o_z;
     G.armnumf = (float)p->armnum; G.cotpitchf = (float)cotpitch;
@@ -411,6 +416,14 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
         CKC(cudaMemsetAsync(*bufs9[q], 0, s9, ctx->st));
     }
     CKC(cudaMalloc(&ctx->rhofloor, (size_t)nc * ctx->esz));
+    CKC(cudaMalloc(&ctx->Zs, 27 * (size_t)(ixmax - 2) * (jymax - 2) * ctx->esz));
+    if (ctx->pair) {
+        float **lo9[] = {&ctx->Ulo, &ctx->U1lo, &ctx->Urawlo};
+        for (int q = 0; q < 3; q++) {
+            CKC(cudaMalloc((void **)lo9[q], s9));
+            CKC(cudaMemsetAsync(*lo9[q], 0, s9, ctx->st));
+        }
+    }
     CKC(cudaMalloc((void **)&ctx->d_sc, sizeof(StepScalars)));
     CKC(cudaMallocHost((void **)&ctx->h_sc, sizeof(StepScalars)));
     memset(ctx->h_sc, 0, sizeof(StepScalars));
@@ -487,8 +500,9 @@ extern "C" int mhd_current_device(int *ordinal)
 /* ------------------------------------------------------------------------ */
 /* transfers                                                                 */
 /* ------------------------------------------------------------------------ */
-/* host FP64 -> device state of the context's type */
-static int put_state(mhd_ctx *ctx, void *dst, const double *src, long long n)
+/* host FP64 -> device state of the context's type; with lo (pair-state
+ * form) each value is split into the nearest FP32 value and the rest */
+static int put_state(mhd_ctx *ctx, void *dst, const double *src, long long n, float *lo = NULL)
 {
     if (!ctx->fp32) {
         CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
@@ -505,13 +519,14 @@ static int put_state(mhd_ctx *ctx, void *dst, const double *src, long long n)
         CK(cudaMemcpyAsync(buf, src + off, m * sizeof(double), cudaMemcpyHostToDevice, ctx->st_cp[b]));
         CK(cudaEventRecord(ctx->ev_cp[b], ctx->st_cp[b]));
         CK(cudaStreamWaitEvent(ctx->st, ctx->ev_cp[b], 0));
-        LAUNCH(PK_CVT, launch_cvt(buf, (float *)dst + off, m, ctx->st));
+        if (lo) LAUNCH(PK_CVT, launch_cvt_pair(buf, (float *)dst + off, lo + off, m, ctx->st));
+        else LAUNCH(PK_CVT, launch_cvt(buf, (float *)dst + off, m, ctx->st));
         CK(cudaEventRecord(ctx->ev_cvt[b], ctx->st));
     }
     return MHD_OK;
 }
 
-static int get_state(mhd_ctx *ctx, double *dst, const void *src, long long n)
+static int get_state(mhd_ctx *ctx, double *dst, const void *src, long long n, const float *lo = NULL)
 {
     if (!ctx->fp32) {
         CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
@@ -524,7 +539,8 @@ static int get_state(mhd_ctx *ctx, double *dst, const void *src, long long n)
         long long m = n - off < ctx->stage_n ? n - off : ctx->stage_n;
         double *buf = ctx->d_stage + b * ctx->stage_n;
         CK(cudaStreamWaitEvent(ctx->st, ctx->ev_cp[b], 0));      /* the buffer's last copy is done */
-        LAUNCH(PK_CVT, launch_cvt_back((const float *)src + off, buf, m, ctx->st));
+        if (lo) LAUNCH(PK_CVT, launch_cvt_pair_back((const float *)src + off, lo + off, buf, m, ctx->st));
+        else LAUNCH(PK_CVT, launch_cvt_back((const float *)src + off, buf, m, ctx->st));
         CK(cudaEventRecord(ctx->ev_cvt[b], ctx->st));
         CK(cudaStreamWaitEvent(ctx->st_cp[b], ctx->ev_cvt[b], 0));
         CK(cudaMemcpyAsync(dst + off, buf, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->st_cp[b]));
@@ -540,7 +556,7 @@ extern "C" int mhd_upload(mhd_ctx *ctx, const double *U, const double *V, const 
     if (!ctx || !U || !V) return MHD_ERR_ARG;
     long long n9 = 9 * ctx->nc;
     int rc;
-    if ((rc = put_state(ctx, ctx->U, U, n9))) return rc;
+    if ((rc = put_state(ctx, ctx->U, U, n9, ctx->Ulo))) return rc;
     ctx->vcur = 0;
     if ((rc = put_state(ctx, ctx->Va, V, n9))) return rc;
     if ((rc = put_state(ctx, ctx->Uinit, Uinit ? Uinit : U, n9))) return rc;
@@ -562,10 +578,12 @@ extern "C" int mhd_upload_state(mhd_ctx *ctx, const double *U, const double *V)
     if (!ctx || !U) return MHD_ERR_ARG;
     if (!ctx->uploaded) return MHD_ERR_STATE;
     int rc;
-    if ((rc = put_state(ctx, ctx->U, U, 9 * ctx->nc))) return rc;
+    if ((rc = put_state(ctx, ctx->U, U, 9 * ctx->nc, ctx->Ulo))) return rc;
     ctx->vcur = 0;
     if (V) {
         if ((rc = put_state(ctx, ctx->Va, V, 9 * ctx->nc))) return rc;
+    } else if (ctx->pair) {
+        LAUNCH(PK_CVT, launch_derive_v_pair(ctx->G, (const float *)ctx->U, ctx->Ulo, (float *)ctx->Va, ctx->st));
     } else if (ctx->fp32) {   /* V = UtoV(U) on the device */
         LAUNCH(PK_CVT, launch_derive_v(ctx->G, (const float *)ctx->U, (float *)ctx->Va, ctx->st));
     } else {
@@ -580,7 +598,7 @@ extern "C" int mhd_download(mhd_ctx *ctx, double *U, double *V)
     if (!ctx) return MHD_ERR_ARG;
     if (!ctx->uploaded) return MHD_ERR_STATE;
     int rc;
-    if (U && (rc = get_state(ctx, U, ctx->U, 9 * ctx->nc))) return rc;
+    if (U && (rc = get_state(ctx, U, ctx->U, 9 * ctx->nc, ctx->Ulo))) return rc;
     if (V && (rc = get_state(ctx, V, vcur_ptr(ctx), 9 * ctx->nc))) return rc;
     CK(cudaStreamSynchronize(ctx->st));
     return MHD_OK;
@@ -693,7 +711,24 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
      * (8 resident blocks of 128 threads per SM in the precision form) */
     a.prefetch = (ctx->upd_tma & 2) ? 8 * ctx->nsm : 0;
     a.wfromu = (ctx->upd_tma & 4) ? 1 : 0;
-    if (ctx->fused == 1) {
+    if (ctx->pair) {
+        /* pair-state form: the split flux kernels of the FP32 form, then the
+         * pair update and boundary fills */
+        if constexpr (sizeof(T) == 4) {
+            PairArgs pa;
+            pa.Unlo = ctx->Ulo; pa.U1lo = ctx->U1lo; pa.Urawlo = ctx->Urawlo;
+            LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
+            LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
+            LAUNCH(PK_FLUX_Z, launch_flux_zsplit(ctx->G, V, Vinit, ctx->d_sc, H, (T *)ctx->Zs, ctx->st));
+            ctx->launches++;   /* two kernels */
+            LAUNCH(PK_UPDATE, launch_update_pair(ctx->G, a, pa, ctx->st));
+            LAUNCH(PK_GHOST, launch_ghost_pair(ctx->G, a, pa, ctx->st));
+            ctx->vcur ^= 1;
+            return MHD_OK;
+        } else {
+            return MHD_ERR_STATE;
+        }
+    } else if (ctx->fused == 1) {
         LAUNCH(PK_STAGE, launch_stage(ctx->G, a, ctx->stage_tj, ctx->stage_seg, ctx->st));
     } else if (ctx->fused == 3) {
         /* the split kernels pipelined over ns slabs of i planes: the fluxes of
@@ -737,15 +772,10 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
     } else {
         LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
         LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
-        /* the z boundary faces (latency-bound) on the side stream, beside the
-         * interior z faces (issue-bound); the update waits for both */
-        CK(cudaEventRecord(ctx->ev_fork, ctx->st));
-        CK(cudaStreamWaitEvent(ctx->st_aux, ctx->ev_fork, 0));
-        CK(launch_zedge(ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), ctx->st_aux));
-        ctx->launches++;
-        CK(cudaEventRecord(ctx->ev_join, ctx->st_aux));
-        LAUNCH(PK_FLUX_Z, launch_flux_zinterior(ctx->G, V, Vinit, ctx->d_sc, H, flux_box(ctx, 2), ctx->st));
-        CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+        /* every z face: the row walk takes the boundary faces along (face 0
+         * on an idle lane, the last face from a per-row scratch) */
+        LAUNCH(PK_FLUX_Z, launch_flux_zsplit(ctx->G, V, Vinit, ctx->d_sc, H, (T *)ctx->Zs, ctx->st));
+        ctx->launches++;   /* two kernels */
         if (ctx->upd_tma == 1)
             LAUNCH(PK_UPDATE, launch_update_tma(ctx->G, a, *ctx->maps, ctx->vcur, &ctx->d_sc->err, ctx->st));
         else
@@ -781,6 +811,7 @@ extern "C" int mhd_tvdrk(mhd_ctx *ctx, double dt, double ch, int counters[3])
     h->psicoef = ctx->p.scheme == MHD_SCHEME_RK2 ? exp(-dt * ch * MHD_ONEOCR * 0.5)
                                                  : exp(-dt * ch * MHD_ONEOCR * MHD_ONEO3);
     h->dtf = (float)h->dt; h->chf = (float)h->ch; h->psif = (float)h->psicoef;
+    h->psifl = (float)(h->psicoef - (double)h->psif);
     h->dtbad = 0;
     CK(cudaMemcpyAsync(ctx->d_sc, h, sizeof(StepScalars), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemsetAsync(ctx->d_cnt, 0, 9 * sizeof(int), ctx->st));
@@ -949,6 +980,7 @@ __global__ void step_scalars_kernel(const MaxLoc *__restrict__ part, int n, doub
     sc->dtf = (float)dt;
     sc->chf = (float)ch;
     sc->psif = (float)sc->psicoef;
+    sc->psifl = (float)(sc->psicoef - (double)sc->psif);
 }
 
 __global__ void advance_t_kernel(StepScalars *sc)
@@ -1116,7 +1148,8 @@ extern "C" int mhd_checkpoint_begin(mhd_ctx *ctx, const char *root, int nout, do
 /* diagnostics                                                               */
 /* ------------------------------------------------------------------------ */
 template <typename T>
-__global__ void __launch_bounds__(256) diag_kernel(Geom G, const T *__restrict__ U, double *part)
+__global__ void __launch_bounds__(256) diag_kernel(Geom G, const T *__restrict__ U, const T *__restrict__ Ulo,
+                                                   double *part)
 {
     __shared__ double sm[5][8];
     const int nj = G.jymax - 2, rows = (G.ixmax - 2) * nj;
@@ -1128,10 +1161,12 @@ __global__ void __launch_bounds__(256) diag_kernel(Geom G, const T *__restrict__
         for (int k = 1 + threadIdx.x; k < G.kzmax - 1; k += blockDim.x) {
             const long long q = cidx(G, i, j, k);
             const double dv = G.dvol[(long long)i * G.kzmax + k];
-            acc[0] += (double)U[q] * dv;
-            acc[1] += (double)U[2 * nc + q] * dv;
-            acc[2] += (double)U[7 * nc + q] * dv;
-            acc[3] += fabs((double)U[8 * nc + q]) * dv;
+            double u0 = U[q], u2 = U[2 * nc + q], u7 = U[7 * nc + q], u8 = U[8 * nc + q];
+            if (Ulo) { u0 += Ulo[q]; u2 += Ulo[2 * nc + q]; u7 += Ulo[7 * nc + q]; u8 += Ulo[8 * nc + q]; }
+            acc[0] += u0 * dv;
+            acc[1] += u2 * dv;
+            acc[2] += u7 * dv;
+            acc[3] += fabs(u8) * dv;
             const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
             double divb = (xp * (double)U[4 * nc + q + si] - xmn * (double)U[4 * nc + q - si]) / (xi * (xp - xmn))
                           + ((double)U[5 * nc + q + sj] - (double)U[5 * nc + q - sj]) / (xi * 2.0 * G.dy)
@@ -1167,8 +1202,8 @@ extern "C" int mhd_diagnostics(mhd_ctx *ctx, mhd_diag *d)
     double *dp = NULL;
     std::vector<double> hp(5 * nblk);
     CK(cudaMallocAsync((void **)&dp, 5 * nblk * sizeof(double), ctx->st));
-    if (ctx->fp32) diag_kernel<float><<<nblk, 256, 0, ctx->st>>>(ctx->G, (const float *)ctx->U, dp);
-    else diag_kernel<double><<<nblk, 256, 0, ctx->st>>>(ctx->G, (const double *)ctx->U, dp);
+    if (ctx->fp32) diag_kernel<float><<<nblk, 256, 0, ctx->st>>>(ctx->G, (const float *)ctx->U, ctx->Ulo, dp);
+    else diag_kernel<double><<<nblk, 256, 0, ctx->st>>>(ctx->G, (const double *)ctx->U, NULL, dp);
     cudaError_t e = cudaGetLastError();
     ctx->launches++;
     if (e == cudaSuccess)
@@ -1202,7 +1237,8 @@ extern "C" int mhd_prof_enable(mhd_ctx *ctx, int on)
 
 extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
 {
-    if (!ctx || fused < 0 || fused > 3 || seg < 1 || (fused != 3 && tj != 7) || (fused == 3 && seg > MHD_MAX_SLABS))
+    if (!ctx || fused < 0 || fused > 3 || seg < 1 || (fused != 3 && tj != 7) || (fused == 3 && seg > MHD_MAX_SLABS) ||
+        (ctx->pair && fused != 0))
         return MHD_ERR_ARG;
     if (fused == 3 && !ctx->st_upd) {
         int lo = 0, hi = 0;
@@ -1226,7 +1262,8 @@ extern "C" int mhd_set_stage_shape(mhd_ctx *ctx, int fused, int tj, int seg)
 
 extern "C" int mhd_set_update_path(mhd_ctx *ctx, int tma)
 {
-    if (!ctx || tma < 0 || tma > 6 || tma == 3 || tma == 5 || (tma == 1 && !ctx->maps) || (tma > 1 && !ctx->fp32))
+    if (!ctx || tma < 0 || tma > 6 || tma == 3 || tma == 5 || (tma == 1 && !ctx->maps) || (tma > 1 && !ctx->fp32) ||
+        (ctx->pair && tma != 0))
         return MHD_ERR_ARG;
     ctx->upd_tma = tma;
     if (ctx->graph_ready) {

@@ -35,6 +35,10 @@ struct mhd_ctx {
     double *dtab;
     float *ftab;
     void *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
+    void *Zs;                    /* the split stage's z walk: 27 values per (i,j) row (boundary-face slots) */
+    /* pair-state form (MHD_PREC_FP32X2): the low words of U, U1 and Uraw */
+    int pair;
+    float *Ulo, *U1lo, *Urawlo;
     int vcur;
     /* stage shape: fused = one kernel for fluxes + update (else the four
      * separate kernels), tile height tj (j) and run length seg (i) */

@@ -3,6 +3,7 @@
  * FP64 repairs written into mhd_dev.cuh (pressure recovery, inner-radius
  * sources, cooling, CFL reduction).
  */
-#include "mhd_kernels.cuh"
+#include "mhd_pair.cuh"
 
 MHD_DEFINE_LAUNCHERS(float)
+MHD_DEFINE_PAIR_LAUNCHERS

@@ -207,6 +207,116 @@ zwalk_flux_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict
     zwalk_row<T, REFLAYOUT>(G, V, sc, F, i, j, flo, fhi);
 }
 
+/* Every z face of the split stage from one walk per (i,j) row.  The
+ * boundary faces' states are slots the walk reconstructs anyway (face_states:
+ * minmod ZLeftVlVzAntisymBzsymBoundary takes the right slot of cell 2 with
+ * v_z negated and the right slot of cell 1 at face 0, ZRightVrFreeBoundary
+ * the left slot of cell kzmax-2 on both sides of face kzmax-2; MC
+ * ZVlrFixedBoundary those slots against Vinit at k = 0 and kzmax-1; van Leer
+ * ZVlrFreeBoundary the one interior slot on both sides; superbee, periodic,
+ * the left slot of cell kzmax-2 and the right slot of cell 1 at both faces).
+ * The walk stores those three slots of each row -- Wl(kzmax-2), Wr(1),
+ * Wr(2) -- in the scratch Zs[rows][27] from the lanes that hold them, and
+ * zlast_flux_kernel forms the two boundary faces of each row from them, one
+ * thread per row.  The interior faces are zwalk_row's.  The states are the
+ * values face_states forms (cell_slots equals recon_slot bit for bit), so the
+ * plain form keeps its bits, and no pass reloads the rows' ends uncoalesced. */
+template <typename T>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1)
+zwalk_edges_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc, T *__restrict__ F,
+                   T *__restrict__ Zs, Box b)
+{
+    /* b: the interior rows i in [1, ixmax-1), j in [1, jymax-1) (indexing
+     * through the box keeps this kernel within 64 registers) */
+    const int nj = b.j1 - b.j0;
+    const long long nrow = (long long)(b.i1 - b.i0) * nj;
+    const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= nrow) return;   /* a whole warp */
+    const int i = b.i0 + (int)(row / nj), j = b.j0 + (int)(row % nj);
+    const int lane = threadIdx.x & 31;
+    const int klast = G.kzmax - 2;
+    const T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
+    T carry[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) carry[m] = T(0.0);
+#pragma unroll 1
+    for (int c0 = 1; c0 <= klast; c0 += 32) {   /* warp-uniform */
+        const int c = c0 + lane;
+        const bool live = c <= klast;
+        T Wl[9], Wr[9], L[9];
+        if (live) cell_slots<T, 2>(G, V, i, j, c, dt, psicoef, Wl, Wr);
+        else {
+#pragma unroll
+            for (int m = 0; m < 9; m++) { Wl[m] = T(0.0); Wr[m] = T(0.0); }
+        }
+        if (c0 == 1 && lane < 2) {   /* the right slots of cells 1 and 2 */
+            T *zr = Zs + row * 27 + 9 + 9 * lane;
+#pragma unroll
+            for (int m = 0; m < 9; m++) zr[m] = Wr[m];
+        }
+        /* the next chunk's carry: the left slot of the chunk's last cell --
+         * in the last chunk, cell kzmax-2, kept past the walk */
+        const int top = min(31, klast - c0);
+#pragma unroll
+        for (int m = 0; m < 9; m++) {
+            const T up = __shfl_up_sync(0xffffffffu, Wl[m], 1);
+            L[m] = lane == 0 ? carry[m] : up;
+            carry[m] = __shfl_sync(0xffffffffu, Wl[m], top);
+        }
+        if (live && c > 1) {
+            T Fo[9];
+            face_flux<T, 2>(G, L, Wr, i, ch, Fo);
+            store_face<T, false>(G, F, i, j, c - 1, Fo);
+        }
+    }
+    if (lane == 0) {   /* the left slot of cell kzmax-2 (the row index recomputed, not held) */
+        T *zr = Zs + ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 27;
+#pragma unroll
+        for (int m = 0; m < 9; m++) zr[m] = carry[m];
+    }
+}
+
+/* The two boundary z faces of each (i,j) row (face 0 and face kzmax-2) from
+ * the slots zwalk_edges_kernel stored: zr[0..8] the left slot of cell
+ * kzmax-2, zr[9..17] the right slot of cell 1, zr[18..26] that of cell 2;
+ * the fills as face_states applies them. */
+template <typename T>
+__global__ void __launch_bounds__(128)
+zlast_flux_kernel(Geom G, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc, T *__restrict__ F,
+                  const T *__restrict__ Zs)
+{
+    const int nj = G.jymax - 2;
+    const long long nrow = (long long)(G.ixmax - 2) * nj;
+    const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrow) return;
+    const int i = 1 + (int)(row / nj), j = 1 + (int)(row % nj);
+    const int lim = G.limiter, klast = G.kzmax - 2;
+    const T ch = Scal<T>::ch(sc);
+    const T *zr = Zs + row * 27;
+    T L[9], R[9], Fo[9];
+    /* face 0 */
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+        R[m] = zr[9 + m];
+        if (lim == MHD_LIMITER_MINMOD) L[m] = m == 3 ? -zr[18 + m] : zr[18 + m];
+        else if (lim == MHD_LIMITER_MC) L[m] = Vinit[(long long)m * G.nc + cidx(G, i, j, 0)];
+        else if (lim == MHD_LIMITER_SUPERBEE) L[m] = zr[m];
+        else L[m] = R[m];
+    }
+    face_flux<T, 2>(G, L, R, i, ch, Fo);
+    store_face<T, false>(G, F, i, j, 0, Fo);
+    /* face kzmax-2 */
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+        L[m] = zr[m];
+        if (lim == MHD_LIMITER_MC) R[m] = Vinit[(long long)m * G.nc + cidx(G, i, j, klast + 1)];
+        else if (lim == MHD_LIMITER_SUPERBEE) R[m] = zr[9 + m];
+        else R[m] = L[m];
+    }
+    face_flux<T, 2>(G, L, R, i, ch, Fo);
+    store_face<T, false>(G, F, i, j, klast, Fo);
+}
+
 /* The two z boundary faces of each (i,j) column (face 0 and face kzmax-2,
  * which take the special left/right states of face_states), one thread per
  * face with the side slowest so every warp takes one branch; the interior
@@ -1159,6 +1269,24 @@ cudaError_t launch_zedge_t(const Geom &G, const T *V, const T *Vinit, const Step
     return cudaGetLastError();
 }
 
+/* every z face of the split stage: the row walk (interior faces, and the
+ * boundary faces' slots into the scratch Zs, 27 values per (i,j) row), then
+ * the two boundary faces of each row; needs at least two interior cells
+ * along z */
+template <typename T>
+cudaError_t launch_flux_zsplit_t(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, T *Zs,
+                                 cudaStream_t st)
+{
+    const long long nrow = (long long)(G.ixmax - 2) * (G.jymax - 2);
+    if (G.kzmax < 4) return cudaErrorInvalidValue;
+    if (nrow <= 0) return cudaSuccess;
+    Box b;
+    b.i0 = 1; b.i1 = G.ixmax - 1; b.j0 = 1; b.j1 = G.jymax - 1; b.k0 = 0; b.k1 = G.kzmax - 1;
+    zwalk_edges_kernel<T><<<nblocks(nrow, 4), 128, 0, st>>>(G, V, sc, F, Zs, b);
+    zlast_flux_kernel<T><<<nblocks(nrow, 128), 128, 0, st>>>(G, Vinit, sc, F, Zs);
+    return cudaGetLastError();
+}
+
 /* dir 2 with edges = false leaves the boundary z faces to launch_zedge_t */
 template <typename T>
 cudaError_t launch_flux_t(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,
@@ -1354,6 +1482,11 @@ cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream
                              cudaStream_t st)                                                                \
     {                                                                                                        \
         return launch_zedge_t<T>(G, V, Vinit, sc, F, b, false, st);                                          \
+    }                                                                                                        \
+    cudaError_t launch_flux_zsplit(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,   \
+                                   T *Zs, cudaStream_t st)                                                   \
+    {                                                                                                        \
+        return launch_flux_zsplit_t<T>(G, V, Vinit, sc, F, Zs, st);                                          \
     }                                                                                                        \
     cudaError_t launch_states(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,     \
                               T *Vl, T *Vr, Box b, cudaStream_t st)                                          \

@@ -55,6 +55,19 @@ struct StageArgs {
     int wfromu = 0;        /* update (precision form): the cell's primitives from UtoV of U^(k), not loaded */
 };
 
+/* pair-state form (MHD_PREC_FP32X2): the low words of the state arrays; the
+ * high words are the FP32 form's arrays in StageArgs<float> */
+struct PairArgs {
+    float *Unlo, *U1lo;   /* U^n and U^(k); the stage output goes to one of them, as its high words do */
+    float *Urawlo;        /* the raw updated state of the cells the boundary fills copy */
+};
+
+cudaError_t launch_update_pair(const Geom &G, const StageArgs<float> &a, const PairArgs &p, cudaStream_t st);
+cudaError_t launch_ghost_pair(const Geom &G, const StageArgs<float> &a, const PairArgs &p, cudaStream_t st);
+cudaError_t launch_cvt_pair(const double *src, float *hi, float *lo, long long n, cudaStream_t st);
+cudaError_t launch_cvt_pair_back(const float *hi, const float *lo, double *dst, long long n, cudaStream_t st);
+cudaError_t launch_derive_v_pair(const Geom &G, const float *U, const float *Ulo, float *V, cudaStream_t st);
+
 #define MHD_DECLARE_LAUNCHERS(T)                                                                             \
     cudaError_t launch_flux(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, \
                             Box b, bool reflayout, cudaStream_t st);                                         \
@@ -64,6 +77,8 @@ struct StageArgs {
                                       T *F, Box b, cudaStream_t st);                                         \
     cudaError_t launch_zedge(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, Box b,  \
                              cudaStream_t st);                                                               \
+    cudaError_t launch_flux_zsplit(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,   \
+                                   T *Zs, cudaStream_t st); /* all z faces, the split stage */              \
     cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                        \
     cudaError_t launch_update_tma(const Geom &G, const StageArgs<T> &a, const UpdMaps &maps, int vpar,      \
                                   int *err, cudaStream_t st); /* precision form only */                    \

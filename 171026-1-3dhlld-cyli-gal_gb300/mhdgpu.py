@@ -22,7 +22,7 @@ MHD_ERR_IO = -8
 LIMITER = {"minmod": 0, "mc": 1, "vanleer": 2, "superbee": 3}
 SOURCE = {"spiral": 0, "axi": 1, "uniformgz": 2, "none": 3}
 SOLVER = {"hlld": 0, "hll": 1}
-PREC = {"fp64": 0, "fp32": 1}
+PREC = {"fp64": 0, "fp32": 1, "fp32x2": 2}
 
 
 class MhdParams(C.Structure):

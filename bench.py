@@ -237,8 +237,8 @@ def precision_report(args):
     # a rounding-sized perturbation of the start alone carries in N steps
     U32 = U.astype(np.float32).astype(np.float64)
     V32 = V.astype(np.float32).astype(np.float64)
-    for prec in ("fp64", "fp32", "fp64_twin", "fp32_storage_floor"):
-        d = M.Disc(grid, with_precision(M, params, "fp32" if prec == "fp32" else "fp64"))
+    for prec in ("fp64", "fp32", "fp32x2", "fp64_twin", "fp32_storage_floor"):
+        d = M.Disc(grid, with_precision(M, params, prec if prec in ("fp32", "fp32x2") else "fp64"))
         if prec == "fp32_storage_floor":
             d.set_state_rounding(True)
         if prec in ("fp64_twin", "fp32_storage_floor"):
@@ -288,6 +288,7 @@ def precision_report(args):
         return {"rel_l1": rl1, "rel_linf": linf, "rel_l1_of_scale": scaled}
 
     out["fp32_vs_fp64"] = compare(res["fp32"])
+    out["fp32x2_vs_fp64"] = compare(res["fp32x2"])
     out["fp64_twin_vs_fp64"] = compare(res["fp64_twin"])
     out["fp32_storage_floor_vs_fp64"] = compare(res["fp32_storage_floor"])
     print(json.dumps(out))
@@ -509,7 +510,7 @@ def select_device(M, local, world):
     return M.current_device()
 
 
-def kernel_bytes(dims, s):
+def kernel_bytes(dims, s, pair=False):
     """Algorithmic bytes per launch of each kernel: its unique inputs and
     outputs, s bytes per value (4 in the precision form, 8 in the plain form).
     A flux kernel reads each cell's 9 primitives once and writes 9 fluxes per
@@ -517,13 +518,15 @@ def kernel_bytes(dims, s):
     with their lower neighbours), U^n, U^(k) in two of the three RK3 stages and
     the density floor, and writes U and V (70 values per cell averaged over
     the stages); the CFL reduction reads 8 primitives of the cells of its
-    range (i < ixmax-11)."""
+    range (i < ixmax-11).  pair: the pair-state form, whose update also moves
+    the low words of U^n, U^(k) and U (94 values per cell averaged: 82, 100,
+    100 by stage)."""
     nx, ny, nz = dims
     zones = nx * ny * nz
     return {"flux_r": (nx + 1) * ny * nz * 18 * s,
             "flux_phi": nx * (ny + 1) * nz * 18 * s,
-            "flux_z": nx * ny * (nz - 1) * 18 * s,      # interior z faces (the boundary faces run beside them)
-            "update": zones * 70 * s,
+            "flux_z": nx * ny * (nz + 1) * 18 * s,      # every z face (the row walk and the boundary faces)
+            "update": zones * (94 if pair else 70) * s,
             "setdt": (nx - 10) * ny * nz * 8 * s,
             "ghost": 0, "trig": 0, "convert": 0,
             "stage": zones * (9 + 9 + 1 + 9 + 9 + 6) * s,
@@ -728,6 +731,23 @@ def main():
                          "what": "mhd_upload_state(U,V) + mhd_step + mhd_download(U,V)"}
     d32.close()
 
+    # ---- pair-state precision form (FP32 fluxes, state as FP32 pairs), resident ----
+    p2 = with_precision(M, params, "fp32x2")
+    d2 = M.Disc(grid, p2)
+    d2.upload(U, V)
+    if dist:
+        dist.barrier()
+    ms2, _, _, _ = time_run(M, d2, args.steps, args.warmup, clocks=False)
+    d2.upload(U, V)
+    _, _, _, kern2, _ = time_steps(M, d2, nprof, 1, prof=True)
+    ms2 = max_over_ranks(dist, ms2)
+    pair = {"value": zones * args.steps * world / (ms2 / 1e3), "unit": "zone-updates/s",
+            "ms_per_step": ms2 / args.steps,
+            "kernels": kernel_rooflines(kern2, kernel_bytes(dims, 4, pair=True), hbm_peak),
+            "what": "MHD_PREC_FP32X2 through mhd_run: the FP32 form's fluxes and primitives, the conserved "
+                    "state as FP32 pairs (hi + lo)"}
+    d2.close()
+
     # ---- plain FP64 form ----
     f64_steps = args.fp64_steps or max(2, min(args.steps, 5))
     p64 = with_precision(M, params, "fp64")
@@ -739,7 +759,7 @@ def main():
     ms64 = max_over_ranks(dist, ms64)
     v64 = zones * f64_steps * world / (ms64 / 1e3)
     fp64 = {"value": v64, "unit": "zone-updates/s", "steps": f64_steps, "ms_per_step": ms64 / f64_steps,
-            "speedup_fp32_over_fp64": value / v64,
+            "speedup_fp32_over_fp64": value / v64, "speedup_pair_over_fp64": pair["value"] / v64,
             "kernels": kernel_rooflines(kern64, kernel_bytes(dims, 8), hbm_peak)}
     link = None
     if not args.no_e2e:
@@ -770,6 +790,7 @@ def main():
                "kernel_share": shares,
                "kernel_roofline": per_kernel,
                "fp64": fp64,
+               "pair": pair,
                "host_link": link,
                "step_traffic": {
                    "split_kernels_gbs": split_bytes / (step_ms / 1e3) / 1e9,

@@ -56,6 +56,11 @@ extern "C" {
 #define MHD_SOURCE_NONE 3     /* NoSource (source.h:308): the geometric terms only */
 #define MHD_PREC_FP64 0       /* plain FP64: bit-identical to the reference C */
 #define MHD_PREC_FP32 1       /* FP32 state and fluxes, FP64 repair of the fragile steps */
+#define MHD_PREC_FP32X2 2     /* MHD_PREC_FP32's FP32 fluxes and primitives, with the conserved state
+                                 held as FP32 pairs (hi + lo, about 48 bits): the state no longer rounds
+                                 to FP32 every stage.  Split stage shape and thread-load update only
+                                 (mhd_set_stage_shape / mhd_set_update_path refuse the others); not in
+                                 the batched form. */
 
 /* Physics and scheme knobs.  Reference: input.h:58-96 (#defines and globals),
  * constant.h:62-79.  gamma=5/3 and cr=0.18 are fixed as in constant.h. */
