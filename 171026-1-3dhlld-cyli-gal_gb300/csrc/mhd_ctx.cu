@@ -167,7 +167,7 @@ static void free_all(mhd_ctx *ctx)
     void *dev[] = {ctx->dtab, ctx->ftab, ctx->U, ctx->U1, ctx->Va, ctx->Vb, ctx->Uinit, ctx->Vinit,
                    ctx->rhofloor, ctx->F, ctx->Gf, ctx->H, ctx->Uraw, ctx->d_sc, ctx->d_trig, ctx->d_trigf,
                    ctx->d_part, ctx->d_cnt, ctx->d_stage, ctx->d_cnt_run, ctx->d_snap, ctx->Ulo, ctx->U1lo,
-                   ctx->Urawlo, ctx->Zs};
+                   ctx->Urawlo, ctx->Zs, ctx->Hb};
     if (ctx->h_snap) cudaFreeHost(ctx->h_snap);
     for (int q = 0; q < NSTAGE; q++) {
         if (ctx->ev_cp[q]) cudaEventDestroy(ctx->ev_cp[q]);
@@ -416,7 +416,8 @@ extern "C" int mhd_create(const mhd_grid *g, const mhd_params *p, mhd_ctx **out)
         CKC(cudaMemsetAsync(*bufs9[q], 0, s9, ctx->st));
     }
     CKC(cudaMalloc(&ctx->rhofloor, (size_t)nc * ctx->esz));
-    CKC(cudaMalloc(&ctx->Zs, 27 * (size_t)(ixmax - 2) * (jymax - 2) * ctx->esz));
+    CKC(cudaMalloc(&ctx->Zs, 18 * (size_t)(ixmax - 2) * (jymax - 2) * ctx->esz));
+    CKC(cudaMalloc(&ctx->Hb, 9 * (size_t)(ixmax - 2) * (jymax - 2) * ctx->esz));
     if (ctx->pair) {
         float **lo9[] = {&ctx->Ulo, &ctx->U1lo, &ctx->Urawlo};
         for (int q = 0; q < 3; q++) {
@@ -693,6 +694,24 @@ static Box flux_box(const mhd_ctx *ctx, int dir)
     return b;
 }
 
+/* The split stage's face fluxes: r, phi, then the z row walk (every z face
+ * but the last of each row, whose slots it leaves in the scratch Zs) and the
+ * last z face of each row into the compact Hb -- and into H as well when the
+ * TMA-staged update, which reads H directly, is selected (Hfull). */
+template <typename T>
+static int split_fluxes(mhd_ctx *ctx, const T *V, const T *Vinit, T *F, T *Gf, T *H, int Hfull)
+{
+    LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
+    LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
+    /* one profiling slot for both z launches: every z face */
+    CK(prof_begin(ctx, PK_FLUX_Z));
+    CK(launch_flux_zwalk(ctx->G, V, Vinit, ctx->d_sc, H, (T *)ctx->Zs, ctx->st));
+    ctx->launches++;
+    CK(launch_flux_zlast(ctx->G, Vinit, ctx->d_sc, H, (T *)ctx->Hb, (const T *)ctx->Zs, Hfull, ctx->st));
+    CK(prof_end(ctx));
+    return MHD_OK;
+}
+
 template <typename T>
 static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
 {
@@ -717,10 +736,8 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
         if constexpr (sizeof(T) == 4) {
             PairArgs pa;
             pa.Unlo = ctx->Ulo; pa.U1lo = ctx->U1lo; pa.Urawlo = ctx->Urawlo;
-            LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
-            LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
-            LAUNCH(PK_FLUX_Z, launch_flux_zsplit(ctx->G, V, Vinit, ctx->d_sc, H, (T *)ctx->Zs, ctx->st));
-            ctx->launches++;   /* two kernels */
+            a.Hb = (const T *)ctx->Hb;
+            if (int rc = split_fluxes<T>(ctx, V, Vinit, F, Gf, H, 0)) return rc;
             LAUNCH(PK_UPDATE, launch_update_pair(ctx->G, a, pa, ctx->st));
             LAUNCH(PK_GHOST, launch_ghost_pair(ctx->G, a, pa, ctx->st));
             ctx->vcur ^= 1;
@@ -770,12 +787,9 @@ static int run_stage(mhd_ctx *ctx, int kind, int last, int *counters)
         LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
         LAUNCH(PK_ZUPDATE, launch_zupdate(ctx->G, a, ctx->st));
     } else {
-        LAUNCH(PK_FLUX_R, launch_flux(0, ctx->G, V, Vinit, ctx->d_sc, F, flux_box(ctx, 0), false, ctx->st));
-        LAUNCH(PK_FLUX_PHI, launch_flux(1, ctx->G, V, Vinit, ctx->d_sc, Gf, flux_box(ctx, 1), false, ctx->st));
-        /* every z face: the row walk takes the boundary faces along (face 0
-         * on an idle lane, the last face from a per-row scratch) */
-        LAUNCH(PK_FLUX_Z, launch_flux_zsplit(ctx->G, V, Vinit, ctx->d_sc, H, (T *)ctx->Zs, ctx->st));
-        ctx->launches++;   /* two kernels */
+        const int hfull = ctx->upd_tma == 1;   /* the TMA-staged update reads H alone */
+        if (!hfull) a.Hb = (const T *)ctx->Hb;
+        if (int rc = split_fluxes<T>(ctx, V, Vinit, F, Gf, H, hfull)) return rc;
         if (ctx->upd_tma == 1)
             LAUNCH(PK_UPDATE, launch_update_tma(ctx->G, a, *ctx->maps, ctx->vcur, &ctx->d_sc->err, ctx->st));
         else

@@ -35,7 +35,8 @@ struct mhd_ctx {
     double *dtab;
     float *ftab;
     void *U, *U1, *Va, *Vb, *Uinit, *Vinit, *rhofloor, *F, *Gf, *H, *Uraw;
-    void *Zs;                    /* the split stage's z walk: 27 values per (i,j) row (boundary-face slots) */
+    void *Zs;                    /* the split stage's z walk: 18 values per (i,j) row (last-face slots) */
+    void *Hb;                    /* the split stage's last z face of each (i,j) row, [9][rows] */
     /* pair-state form (MHD_PREC_FP32X2): the low words of U, U1 and Uraw */
     int pair;
     float *Ulo, *U1lo, *Urawlo;

@@ -215,16 +215,23 @@ zwalk_flux_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict
  * ZVlrFixedBoundary those slots against Vinit at k = 0 and kzmax-1; van Leer
  * ZVlrFreeBoundary the one interior slot on both sides; superbee, periodic,
  * the left slot of cell kzmax-2 and the right slot of cell 1 at both faces).
- * The walk stores those three slots of each row -- Wl(kzmax-2), Wr(1),
- * Wr(2) -- in the scratch Zs[rows][27] from the lanes that hold them, and
- * zlast_flux_kernel forms the two boundary faces of each row from them, one
- * thread per row.  The interior faces are zwalk_row's.  The states are the
- * values face_states forms (cell_slots equals recon_slot bit for bit), so the
- * plain form keeps its bits, and no pass reloads the rows' ends uncoalesced. */
+ *   Face 0 is the face c-1 of the first chunk's lane 0, otherwise idle, so
+ * its flux is stored with the chunk's other faces (lane 1's right slot comes
+ * by a shuffle); for superbee its left slot is in the last chunk, so the
+ * face is left to zlast_flux_kernel.
+ *   Face kzmax-2 needs one face evaluation more than whole 32-lane chunks
+ * hold: the walk keeps the left slot of cell kzmax-2 (the last chunk's
+ * carry) and, for superbee, the right slot of cell 1 in the scratch
+ * Zs[18][rows], and zlast_flux_kernel forms that face, one thread per row,
+ * into the compact Hb[9][rows] that the update reads for its cells k =
+ * kzmax-2 -- a coalesced store where writing H at (i, j, kzmax-2) would touch
+ * one 32-byte sector per row and variable.
+ * The states are the values face_states forms (cell_slots equals recon_slot
+ * bit for bit), so the plain form keeps its bits. */
 template <typename T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 1)
-zwalk_edges_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restrict__ sc, T *__restrict__ F,
-                   T *__restrict__ Zs, Box b)
+zwalk_edges_kernel(Geom G, const T *__restrict__ V, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc,
+                   T *__restrict__ F, T *__restrict__ Zs, Box b)
 {
     /* b: the interior rows i in [1, ixmax-1), j in [1, jymax-1) (indexing
      * through the box keeps this kernel within 64 registers) */
@@ -234,7 +241,7 @@ zwalk_edges_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restric
     if (row >= nrow) return;   /* a whole warp */
     const int i = b.i0 + (int)(row / nj), j = b.j0 + (int)(row % nj);
     const int lane = threadIdx.x & 31;
-    const int klast = G.kzmax - 2;
+    const int klast = G.kzmax - 2, lim = G.limiter;
     const T dt = Scal<T>::dt(sc), ch = Scal<T>::ch(sc), psicoef = Scal<T>::psi(sc);
     T carry[9];
 #pragma unroll
@@ -249,11 +256,6 @@ zwalk_edges_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restric
 #pragma unroll
             for (int m = 0; m < 9; m++) { Wl[m] = T(0.0); Wr[m] = T(0.0); }
         }
-        if (c0 == 1 && lane < 2) {   /* the right slots of cells 1 and 2 */
-            T *zr = Zs + row * 27 + 9 + 9 * lane;
-#pragma unroll
-            for (int m = 0; m < 9; m++) zr[m] = Wr[m];
-        }
         /* the next chunk's carry: the left slot of the chunk's last cell --
          * in the last chunk, cell kzmax-2, kept past the walk */
         const int top = min(31, klast - c0);
@@ -263,27 +265,55 @@ zwalk_edges_kernel(Geom G, const T *__restrict__ V, const StepScalars *__restric
             L[m] = lane == 0 ? carry[m] : up;
             carry[m] = __shfl_sync(0xffffffffu, Wl[m], top);
         }
-        if (live && c > 1) {
+        bool face = live && c > 1;
+        if (c0 == 1) {   /* face 0 on lane 0 */
+            if (lim == MHD_LIMITER_MINMOD) {
+#pragma unroll
+                for (int m = 0; m < 9; m++) {
+                    const T w2 = __shfl_down_sync(0xffffffffu, Wr[m], 1);
+                    if (lane == 0) L[m] = m == 3 ? -w2 : w2;
+                }
+            } else if (lane == 0) {
+                const long long q0 = cidx(G, i, j, 0);
+#pragma unroll
+                for (int m = 0; m < 9; m++)
+                    L[m] = lim == MHD_LIMITER_MC ? Vinit[(long long)m * G.nc + q0] : Wr[m];
+            }
+            if (lane == 0) {
+                if (lim == MHD_LIMITER_SUPERBEE) {
+#pragma unroll
+                    for (int m = 0; m < 9; m++) Zs[(9 + m) * nrow + row] = Wr[m];
+                } else {
+                    face = live;
+                }
+            }
+        }
+        if (face) {
             T Fo[9];
             face_flux<T, 2>(G, L, Wr, i, ch, Fo);
             store_face<T, false>(G, F, i, j, c - 1, Fo);
         }
     }
     if (lane == 0) {   /* the left slot of cell kzmax-2 (the row index recomputed, not held) */
-        T *zr = Zs + ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 27;
+        T *zr = Zs + ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
 #pragma unroll
-        for (int m = 0; m < 9; m++) zr[m] = carry[m];
+        for (int m = 0; m < 9; m++) zr[m * nrow] = carry[m];
     }
 }
 
-/* The two boundary z faces of each (i,j) row (face 0 and face kzmax-2) from
- * the slots zwalk_edges_kernel stored: zr[0..8] the left slot of cell
- * kzmax-2, zr[9..17] the right slot of cell 1, zr[18..26] that of cell 2;
- * the fills as face_states applies them. */
+/* The last z face (kzmax-2) of each (i,j) row from the slots
+ * zwalk_edges_kernel stored in Zs[18][rows] (rows 0..8 the left slot of cell
+ * kzmax-2; 9..17, superbee only, the right slot of cell 1), with the fills of
+ * face_states: the right state is the left one (minmod ZRightVrFreeBoundary,
+ * van Leer ZVlrFreeBoundary), Vinit at kzmax-1 (MC ZVlrFixedBoundary) or the
+ * right slot of cell 1 (superbee, periodic, where face 0 takes the same two
+ * states and so the same flux).  One thread per row; the flux goes to the
+ * compact Hb[9][rows] (coalesced) and, where H must hold every face (Hfull:
+ * the TMA-staged update reads H directly) or for superbee's face 0, into H. */
 template <typename T>
 __global__ void __launch_bounds__(128)
-zlast_flux_kernel(Geom G, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc, T *__restrict__ F,
-                  const T *__restrict__ Zs)
+zlast_flux_kernel(Geom G, const T *__restrict__ Vinit, const StepScalars *__restrict__ sc, T *__restrict__ H,
+                  T *__restrict__ Hb, const T *__restrict__ Zs, int Hfull)
 {
     const int nj = G.jymax - 2;
     const long long nrow = (long long)(G.ixmax - 2) * nj;
@@ -291,30 +321,19 @@ zlast_flux_kernel(Geom G, const T *__restrict__ Vinit, const StepScalars *__rest
     if (row >= nrow) return;
     const int i = 1 + (int)(row / nj), j = 1 + (int)(row % nj);
     const int lim = G.limiter, klast = G.kzmax - 2;
-    const T ch = Scal<T>::ch(sc);
-    const T *zr = Zs + row * 27;
     T L[9], R[9], Fo[9];
-    /* face 0 */
 #pragma unroll
     for (int m = 0; m < 9; m++) {
-        R[m] = zr[9 + m];
-        if (lim == MHD_LIMITER_MINMOD) L[m] = m == 3 ? -zr[18 + m] : zr[18 + m];
-        else if (lim == MHD_LIMITER_MC) L[m] = Vinit[(long long)m * G.nc + cidx(G, i, j, 0)];
-        else if (lim == MHD_LIMITER_SUPERBEE) L[m] = zr[m];
-        else L[m] = R[m];
-    }
-    face_flux<T, 2>(G, L, R, i, ch, Fo);
-    store_face<T, false>(G, F, i, j, 0, Fo);
-    /* face kzmax-2 */
-#pragma unroll
-    for (int m = 0; m < 9; m++) {
-        L[m] = zr[m];
+        L[m] = Zs[m * nrow + row];
         if (lim == MHD_LIMITER_MC) R[m] = Vinit[(long long)m * G.nc + cidx(G, i, j, klast + 1)];
-        else if (lim == MHD_LIMITER_SUPERBEE) R[m] = zr[9 + m];
+        else if (lim == MHD_LIMITER_SUPERBEE) R[m] = Zs[(9 + m) * nrow + row];
         else R[m] = L[m];
     }
-    face_flux<T, 2>(G, L, R, i, ch, Fo);
-    store_face<T, false>(G, F, i, j, klast, Fo);
+    face_flux<T, 2>(G, L, R, i, Scal<T>::ch(sc), Fo);
+#pragma unroll
+    for (int m = 0; m < 9; m++) Hb[m * nrow + row] = Fo[m];
+    if (Hfull) store_face<T, false>(G, H, i, j, klast, Fo);
+    if (lim == MHD_LIMITER_SUPERBEE) store_face<T, false>(G, H, i, j, 0, Fo);
 }
 
 /* The two z boundary faces of each (i,j) column (face 0 and face kzmax-2,
@@ -529,12 +548,20 @@ __device__ __forceinline__ int update_cell(const Geom &G, const StageArgs<T> &a,
 {
     const long long nc = G.nc, q = cidx(G, i, j, k);
     const long long si = (long long)G.jymax * G.kzmax, sj = G.kzmax;
+    /* the upper z face of the last cell of a row from the compact Hb, where
+     * the split stage keeps it */
+    const T *hu = a.H + q;
+    long long hs = nc;
+    if (a.Hb && k == G.kzmax - 2) {
+        hu = a.Hb + (long long)(i - 1) * (G.jymax - 2) + (j - 1);
+        hs = (long long)(G.ixmax - 2) * (G.jymax - 2);
+    }
     T g[6], div[9];
     geo_factors<T>(G, i, k, g);
 #pragma unroll
     for (int m = 0; m < 9; m++) {
         const long long mq = m * nc + q;
-        div[m] = flux_div<T>(g, a.F[mq], a.F[mq - si], a.G[mq], a.G[mq - sj], a.H[mq], a.H[mq - 1]);
+        div[m] = flux_div<T>(g, a.F[mq], a.F[mq - si], a.G[mq], a.G[mq - sj], hu[m * hs], a.H[mq - 1]);
     }
     return update_apply<T>(G, a, i, j, k, div);
 }
@@ -1269,21 +1296,31 @@ cudaError_t launch_zedge_t(const Geom &G, const T *V, const T *Vinit, const Step
     return cudaGetLastError();
 }
 
-/* every z face of the split stage: the row walk (interior faces, and the
- * boundary faces' slots into the scratch Zs, 27 values per (i,j) row), then
- * the two boundary faces of each row; needs at least two interior cells
- * along z */
+/* the split stage's z faces: the row walk (the interior faces, and the
+ * boundary faces' slots into the scratch Zs, 27 values per (i,j) row);
+ * needs at least two interior cells along z */
 template <typename T>
-cudaError_t launch_flux_zsplit_t(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, T *Zs,
-                                 cudaStream_t st)
+cudaError_t launch_flux_zwalk_t(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, T *Zs,
+                                cudaStream_t st)
 {
     const long long nrow = (long long)(G.ixmax - 2) * (G.jymax - 2);
     if (G.kzmax < 4) return cudaErrorInvalidValue;
     if (nrow <= 0) return cudaSuccess;
     Box b;
     b.i0 = 1; b.i1 = G.ixmax - 1; b.j0 = 1; b.j1 = G.jymax - 1; b.k0 = 0; b.k1 = G.kzmax - 1;
-    zwalk_edges_kernel<T><<<nblocks(nrow, 4), 128, 0, st>>>(G, V, sc, F, Zs, b);
-    zlast_flux_kernel<T><<<nblocks(nrow, 128), 128, 0, st>>>(G, Vinit, sc, F, Zs);
+    zwalk_edges_kernel<T><<<nblocks(nrow, 4), 128, 0, st>>>(G, V, Vinit, sc, F, Zs, b);
+    return cudaGetLastError();
+}
+
+/* ... and the last face of each row from that scratch, into Hb (and H with
+ * Hfull) */
+template <typename T>
+cudaError_t launch_flux_zlast_t(const Geom &G, const T *Vinit, const StepScalars *sc, T *H, T *Hb, const T *Zs,
+                                int Hfull, cudaStream_t st)
+{
+    const long long nrow = (long long)(G.ixmax - 2) * (G.jymax - 2);
+    if (nrow <= 0) return cudaSuccess;
+    zlast_flux_kernel<T><<<nblocks(nrow, 128), 128, 0, st>>>(G, Vinit, sc, H, Hb, Zs, Hfull);
     return cudaGetLastError();
 }
 
@@ -1483,10 +1520,15 @@ cudaError_t launch_cvt_back_t(const T *src, double *dst, long long n, cudaStream
     {                                                                                                        \
         return launch_zedge_t<T>(G, V, Vinit, sc, F, b, false, st);                                          \
     }                                                                                                        \
-    cudaError_t launch_flux_zsplit(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,   \
-                                   T *Zs, cudaStream_t st)                                                   \
+    cudaError_t launch_flux_zwalk(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,    \
+                                  T *Zs, cudaStream_t st)                                                    \
     {                                                                                                        \
-        return launch_flux_zsplit_t<T>(G, V, Vinit, sc, F, Zs, st);                                          \
+        return launch_flux_zwalk_t<T>(G, V, Vinit, sc, F, Zs, st);                                           \
+    }                                                                                                        \
+    cudaError_t launch_flux_zlast(const Geom &G, const T *Vinit, const StepScalars *sc, T *H, T *Hb,        \
+                                  const T *Zs, int Hfull, cudaStream_t st)                                   \
+    {                                                                                                        \
+        return launch_flux_zlast_t<T>(G, Vinit, sc, H, Hb, Zs, Hfull, st);                                   \
     }                                                                                                        \
     cudaError_t launch_states(int dir, const Geom &G, const T *V, const T *Vinit, const StepScalars *sc,     \
                               T *Vl, T *Vr, Box b, cudaStream_t st)                                          \

@@ -53,6 +53,7 @@ struct StageArgs {
     int prefetch = 0;      /* update: blocks ahead whose streamed inputs each block prefetches into L2 (0: none) */
     int ibeg = 1, iend = 0;  /* update: the planes i in [ibeg, iend) it covers (iend 0: through ixmax-2) */
     int wfromu = 0;        /* update (precision form): the cell's primitives from UtoV of U^(k), not loaded */
+    const T *Hb = nullptr; /* update: the last z face of each row, [9][rows] (split stage), else in H */
 };
 
 /* pair-state form (MHD_PREC_FP32X2): the low words of the state arrays; the
@@ -77,8 +78,10 @@ cudaError_t launch_derive_v_pair(const Geom &G, const float *U, const float *Ulo
                                       T *F, Box b, cudaStream_t st);                                         \
     cudaError_t launch_zedge(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F, Box b,  \
                              cudaStream_t st);                                                               \
-    cudaError_t launch_flux_zsplit(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,   \
-                                   T *Zs, cudaStream_t st); /* all z faces, the split stage */              \
+    cudaError_t launch_flux_zwalk(const Geom &G, const T *V, const T *Vinit, const StepScalars *sc, T *F,    \
+                                  T *Zs, cudaStream_t st); /* split stage: z faces 0 .. kzmax-3 */          \
+    cudaError_t launch_flux_zlast(const Geom &G, const T *Vinit, const StepScalars *sc, T *H, T *Hb,        \
+                                  const T *Zs, int Hfull, cudaStream_t st); /* ... face kzmax-2 */          \
     cudaError_t launch_update(const Geom &G, const StageArgs<T> &a, cudaStream_t st);                        \
     cudaError_t launch_update_tma(const Geom &G, const StageArgs<T> &a, const UpdMaps &maps, int vpar,      \
                                   int *err, cudaStream_t st); /* precision form only */                    \

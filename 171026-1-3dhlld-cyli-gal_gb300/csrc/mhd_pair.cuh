@@ -203,13 +203,20 @@ __device__ __forceinline__ int update_cell_pair(const Geom &G, const StageArgs<f
     const StageCoef kc = stage_coef(kind);
     const float ch = kind == 2 ? MHD_ONEO3_HI : kc.c, cl = kind == 2 ? MHD_ONEO3_LO : 0.0f;
     float g[6], div[9], W[9], S[9], uh[9], ul[9];
-    /* in three phases, as the FP32 update: the flux divergence (54 loads),
-     * the primitives and sources, then the pair states and the combination */
+    /* in three phases, as the FP32 update: the flux divergence (54 loads;
+     * the last z face of a row from the compact Hb), the primitives and
+     * sources, then the pair states and the combination */
+    const float *hu = a.H + q;
+    long long hs = nc;
+    if (a.Hb && k == G.kzmax - 2) {
+        hu = a.Hb + (long long)(i - 1) * (G.jymax - 2) + (j - 1);
+        hs = (long long)(G.ixmax - 2) * (G.jymax - 2);
+    }
     geo_factors<float>(G, i, k, g);
 #pragma unroll
     for (int m = 0; m < 9; m++) {
         const long long mq = m * nc + q;
-        div[m] = flux_div<float>(g, a.F[mq], a.F[mq - si], a.G[mq], a.G[mq - sj], a.H[mq], a.H[mq - 1]);
+        div[m] = flux_div<float>(g, a.F[mq], a.F[mq - si], a.G[mq], a.G[mq - sj], hu[m * hs], a.H[mq - 1]);
     }
 #pragma unroll
     for (int m = 0; m < 9; m++) W[m] = a.V[m * nc + q];

@@ -525,7 +525,7 @@ def kernel_bytes(dims, s, pair=False):
     zones = nx * ny * nz
     return {"flux_r": (nx + 1) * ny * nz * 18 * s,
             "flux_phi": nx * (ny + 1) * nz * 18 * s,
-            "flux_z": nx * ny * (nz + 1) * 18 * s,      # every z face (the row walk and the boundary faces)
+            "flux_z": nx * ny * (nz + 1) * 18 * s,      # every z face (the row walk and the last face of each row)
             "update": zones * (94 if pair else 70) * s,
             "setdt": (nx - 10) * ny * nz * 8 * s,
             "ghost": 0, "trig": 0, "convert": 0,
