@@ -315,6 +315,8 @@ int mhd_dbg_gravity(mhd_ctx *ctx, double *gr);
 
 /* ---- batched form: many independent discs ------------------------------- */
 typedef struct mhd_batch mhd_batch;
+/* One precision (MHD_PREC_FP64 or MHD_PREC_FP32; MHD_PREC_FP32X2 is refused
+ * with MHD_ERR_ARG) and one RK scheme for all n discs. */
 int mhd_batch_create(int n, const mhd_grid *grids, const mhd_params *params, mhd_batch **out);
 void mhd_batch_destroy(mhd_batch *b);
 int mhd_batch_upload(mhd_batch *b, int disc, const double *U, const double *V,
