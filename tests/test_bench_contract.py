@@ -130,7 +130,13 @@ def test_default_line_has_the_contract_keys(bench_with_stand_in, monkeypatch, ca
     for k in ("flux_r", "flux_phi", "flux_z", "update", "setdt"):
         assert kr[k]["frac_hbm"] == pytest.approx(kr[k]["gbs"] / r["peak"])
     assert kr["flux_r"]["bytes_per_launch"] == 25 * 16 * 20 * 18 * 4
+    assert kr["flux_z"]["bytes_per_launch"] == 24 * 16 * 21 * 18 * 4   # every z face, the boundary ones too
     assert kr["setdt"]["bytes_per_launch"] == 14 * 16 * 20 * 8 * 4
+    p2 = d["pair"]
+    assert p2["unit"] == d["unit"] and p2["ms_per_step"] == pytest.approx(2.0)
+    assert p2["value"] == pytest.approx(zones / 2e-3)
+    assert p2["kernels"]["update"]["bytes_per_launch"] == zones * 94 * 4
+    assert f_speedups_ok(d)
     f = d["fp64"]
     assert f["e2e"]["unit"] == d["unit"] and f["e2e"]["h2d_bytes_per_step"] == e["with_v"]["h2d_bytes_per_step"]
     assert f["kernels"]["update"]["bytes_per_launch"] == zones * 70 * 8
@@ -138,6 +144,12 @@ def test_default_line_has_the_contract_keys(bench_with_stand_in, monkeypatch, ca
     assert hl["bytes"] == e["with_v"]["h2d_bytes_per_step"] and hl["h2d_gbs"] == pytest.approx(hl["bytes"] / 1e-3 / 1e9)
     st = d["step_traffic"]
     assert st["fused_minimum_gbs"] == pytest.approx(300 * zones / 2e-3 / 1e9)
+
+
+def f_speedups_ok(d):
+    f = d["fp64"]
+    return (f["speedup_fp32_over_fp64"] == pytest.approx(d["value"] / f["value"])
+            and f["speedup_pair_over_fp64"] == pytest.approx(d["pair"]["value"] / f["value"]))
 
 
 def test_reference_arm_line(monkeypatch, capsys):
