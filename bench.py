@@ -760,7 +760,9 @@ def main():
     v64 = zones * f64_steps * world / (ms64 / 1e3)
     fp64 = {"value": v64, "unit": "zone-updates/s", "steps": f64_steps, "ms_per_step": ms64 / f64_steps,
             "speedup_fp32_over_fp64": value / v64, "speedup_pair_over_fp64": pair["value"] / v64,
-            "kernels": kernel_rooflines(kern64, kernel_bytes(dims, 8), hbm_peak)}
+            "kernels": kernel_rooflines(kern64, kernel_bytes(dims, 8), hbm_peak),
+            "bound": "FP64 pipe: the flux kernels keep it 86 % active (ncu, profiles/flux_fp64_256x256x128.md); "
+                     "frac_hbm is each kernel's HBM fraction only"}
     link = None
     if not args.no_e2e:
         d64.upload(U, V)
