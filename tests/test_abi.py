@@ -79,3 +79,11 @@ def test_device_selection_errors_are_codes(M):
         assert rc0 == 0 and L.mhd_use_device(-1) == -1 and L.mhd_use_device(1 << 20) == -1
         assert L.mhd_current_device(C.byref(d)) == 0 and d.value == 0
     assert L.mhd_current_device(None) == -1
+
+
+def test_binding_precision_codes_match_the_header(M):
+    """The binding's precision names map to the header's MHD_PREC_* codes."""
+    src = open(os.path.join(ROOT, "include", "mhd_gpu.h")).read()
+    codes = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define MHD_PREC_(\w+) (\d+)", src)}
+    assert codes == {"FP64": 0, "FP32": 1, "FP32X2": 2}
+    assert M.PREC == {k.lower(): v for k, v in codes.items()}
